@@ -1,0 +1,297 @@
+"""forkmatch_gb300 -- Python binding of libforkmatch (GB300-native ForkMatch).
+
+Thin ctypes mirror of ``include/forkmatch.h``.  The library is loaded from
+``forkmatch_gb300/lib/libforkmatch.so`` (built in-tree by
+``forkmatch_gb300.build``); there is no fallback: if it is missing, importing
+``lib()`` raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libforkmatch.so")
+CLI_PATH = os.path.join(HERE, "lib", "ForkMatch")
+MAXQ = 32
+
+FM_OK = 0
+FM_ERR_OUTPUT_OVERFLOW = 12
+MODE_TABLE, MODE_COUNT = 0, 1
+COLUMNS_REFERENCE, COLUMNS_QUERY_ID = 0, 1
+
+STATUS_NAMES = {
+    0: "FM_OK", 1: "FM_ERR_ARG", 2: "FM_ERR_IO", 3: "FM_ERR_DATA_HEADER0", 4: "FM_ERR_DATA_TRAILER",
+    5: "FM_ERR_DATA_HEADER", 6: "FM_ERR_DATA_LINE", 7: "FM_ERR_QUERY_FORMAT", 8: "FM_ERR_QUERY_MISSING",
+    9: "FM_ERR_DISCONNECTED", 10: "FM_ERR_UNSUPPORTED", 11: "FM_ERR_POOL", 12: "FM_ERR_OUTPUT_OVERFLOW",
+    13: "FM_ERR_CUDA", 14: "FM_ERR_DEVICE", 15: "FM_ERR_NOMEM",
+}
+
+# Every function include/forkmatch.h declares (checked by the CPU test suite).
+EXPORTS = [
+    "fm_status_string", "fm_last_error", "fm_knobs_default", "fm_context_create", "fm_context_destroy",
+    "fm_context_stream", "fm_graph_load_file", "fm_graph_load_text", "fm_graph_from_edges", "fm_graph_get_info",
+    "fm_graph_free", "fm_query_compile_file", "fm_query_compile_text", "fm_query_get_info", "fm_query_free",
+    "fm_match_opts_default", "fm_match", "fm_host_alloc", "fm_host_free", "fm_version", "fm_device_count",
+]
+
+
+class Knobs(ctypes.Structure):
+    _fields_ = [("prealloc_bytes", ctypes.c_uint64), ("soln_prealloc_bytes", ctypes.c_uint64),
+                ("output_prealloc_bytes", ctypes.c_uint64), ("bank_rows", ctypes.c_uint32),
+                ("device", ctypes.c_int32)]
+
+
+class GraphInfo(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.c_uint32), ("label_slots", ctypes.c_uint32), ("edges", ctypes.c_uint64),
+                ("segments", ctypes.c_uint64), ("long_segments", ctypes.c_uint64), ("nbr_words", ctypes.c_uint64),
+                ("max_list", ctypes.c_uint32), ("has_duplicates", ctypes.c_int32), ("device_bytes", ctypes.c_uint64),
+                ("build_ms", ctypes.c_double)]
+
+
+_U32Q = ctypes.c_uint32 * MAXQ
+
+
+class QueryInfo(ctypes.Structure):
+    _fields_ = [("q", ctypes.c_uint32), ("e_lines", ctypes.c_uint32), ("max_valency", ctypes.c_uint32),
+                ("order", _U32Q), ("local_of_depth", _U32Q), ("inv", _U32Q), ("nreq", _U32Q),
+                ("req_climb", _U32Q * MAXQ), ("req_label", _U32Q * MAXQ), ("req_refl", _U32Q * MAXQ),
+                ("pk_dist", _U32Q), ("automorphisms", ctypes.c_uint64)]
+
+
+class MatchOpts(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("columns", ctypes.c_int32), ("stream", ctypes.c_void_p),
+                ("host_rows", ctypes.c_void_p), ("host_rows_cap", ctypes.c_uint64),
+                ("root_begin", ctypes.c_uint32), ("root_end", ctypes.c_uint32), ("profile", ctypes.c_int32)]
+
+
+class LevelStats(ctypes.Structure):
+    _fields_ = [("parents", ctypes.c_uint64), ("lookups", ctypes.c_uint64), ("list_words", ctypes.c_uint64),
+                ("produced", ctypes.c_uint64), ("launches", ctypes.c_uint32), ("kernel_ms", ctypes.c_double)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_uint64), ("rows", ctypes.c_uint64), ("rows_device", ctypes.c_void_p),
+                ("rows_copied", ctypes.c_uint64), ("truncated", ctypes.c_int32), ("q", ctypes.c_uint32),
+                ("device_ms", ctypes.c_double), ("launches", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64),
+                ("d2h_bytes", ctypes.c_uint64), ("level", LevelStats * MAXQ)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libforkmatch.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libforkmatch.so not built: run forkmatch_gb300.build.build() (no fallback exists)")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, u32, u64, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32
+        L.fm_status_string.restype = ctypes.c_char_p
+        L.fm_status_string.argtypes = [i32]
+        L.fm_last_error.restype = ctypes.c_char_p
+        L.fm_version.restype = ctypes.c_char_p
+        L.fm_knobs_default.argtypes = [ctypes.POINTER(Knobs)]
+        L.fm_context_create.argtypes = [ctypes.POINTER(Knobs), ctypes.POINTER(vp)]
+        L.fm_context_destroy.argtypes = [vp]
+        L.fm_context_stream.argtypes = [vp]
+        L.fm_context_stream.restype = vp
+        L.fm_graph_load_file.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(vp)]
+        L.fm_graph_load_text.argtypes = [vp, ctypes.c_char_p, u64, ctypes.POINTER(vp)]
+        L.fm_graph_from_edges.argtypes = [vp, u32, u32, u64, vp, vp, vp, ctypes.POINTER(vp)]
+        L.fm_graph_get_info.argtypes = [vp, ctypes.POINTER(GraphInfo)]
+        L.fm_graph_free.argtypes = [vp]
+        L.fm_query_compile_file.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
+        L.fm_query_compile_text.argtypes = [ctypes.c_char_p, u64, ctypes.POINTER(vp)]
+        L.fm_query_get_info.argtypes = [vp, ctypes.POINTER(QueryInfo)]
+        L.fm_query_free.argtypes = [vp]
+        L.fm_match_opts_default.argtypes = [ctypes.POINTER(MatchOpts)]
+        L.fm_match.argtypes = [vp, vp, vp, ctypes.POINTER(MatchOpts), ctypes.POINTER(Result)]
+        L.fm_host_alloc.argtypes = [u64]
+        L.fm_host_alloc.restype = vp
+        L.fm_host_free.argtypes = [vp]
+        _lib = L
+    return _lib
+
+
+class FMError(RuntimeError):
+    def __init__(self, status, what):
+        msg = lib().fm_last_error().decode(errors="replace")
+        super().__init__("%s: %s (%s)" % (what, STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+def _check(st, what, allow=()):
+    if st != FM_OK and st not in allow:
+        raise FMError(st, what)
+    return st
+
+
+def default_knobs(**overrides):
+    k = Knobs()
+    lib().fm_knobs_default(ctypes.byref(k))
+    for name, v in overrides.items():
+        setattr(k, name, v)
+    return k
+
+
+class Context:
+    """Device slab + stream (the reference's PREALLOC slab)."""
+
+    def __init__(self, knobs=None, **overrides):
+        k = knobs if knobs is not None else default_knobs(**overrides)
+        h = ctypes.c_void_p()
+        _check(lib().fm_context_create(ctypes.byref(k), ctypes.byref(h)), "fm_context_create")
+        self._h = h
+        self.knobs = k
+
+    @property
+    def stream(self):
+        return lib().fm_context_stream(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fm_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Graph:
+    """Resident device data graph."""
+
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self._h = handle
+
+    @classmethod
+    def from_edges(cls, ctx, V, label_slots, src, dst, label):
+        src = np.ascontiguousarray(src, dtype=np.uint32)
+        dst = np.ascontiguousarray(dst, dtype=np.uint32)
+        label = np.ascontiguousarray(label, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        _check(lib().fm_graph_from_edges(ctx._h, V, label_slots, len(src), src.ctypes.data, dst.ctypes.data,
+                                         label.ctypes.data, ctypes.byref(h)), "fm_graph_from_edges")
+        return cls(ctx, h)
+
+    @classmethod
+    def from_text(cls, ctx, text):
+        if isinstance(text, str):
+            text = text.encode()
+        h = ctypes.c_void_p()
+        _check(lib().fm_graph_load_text(ctx._h, text, len(text), ctypes.byref(h)), "fm_graph_load_text")
+        return cls(ctx, h)
+
+    @classmethod
+    def from_file(cls, ctx, path):
+        h = ctypes.c_void_p()
+        _check(lib().fm_graph_load_file(ctx._h, os.fsencode(path), ctypes.byref(h)), "fm_graph_load_file")
+        return cls(ctx, h)
+
+    def info(self):
+        gi = GraphInfo()
+        _check(lib().fm_graph_get_info(self._h, ctypes.byref(gi)), "fm_graph_get_info")
+        return gi
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fm_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Query:
+    """Compiled query (reference matching order and requirements)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def from_text(cls, text):
+        if isinstance(text, str):
+            text = text.encode()
+        h = ctypes.c_void_p()
+        _check(lib().fm_query_compile_text(text, len(text), ctypes.byref(h)), "fm_query_compile_text")
+        return cls(h)
+
+    @classmethod
+    def from_file(cls, path):
+        h = ctypes.c_void_p()
+        _check(lib().fm_query_compile_file(os.fsencode(path), ctypes.byref(h)), "fm_query_compile_file")
+        return cls(h)
+
+    def info(self):
+        qi = QueryInfo()
+        _check(lib().fm_query_get_info(self._h, ctypes.byref(qi)), "fm_query_get_info")
+        return qi
+
+    @property
+    def q(self):
+        return self.info().q
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fm_query_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class PinnedRows:
+    """Pinned host buffer for embedding rows (fm_host_alloc)."""
+
+    def __init__(self, rows, q):
+        self.cap = int(rows)
+        self.q = int(q)
+        self.ptr = lib().fm_host_alloc(max(1, self.cap * self.q * 4))
+        if not self.ptr:
+            raise MemoryError("fm_host_alloc failed")
+        self.array = np.ctypeslib.as_array(ctypes.cast(self.ptr, ctypes.POINTER(ctypes.c_uint32)),
+                                           shape=(max(1, self.cap * self.q),))[: self.cap * self.q]
+
+    def view(self, n):
+        return self.array[: n * self.q].reshape(n, self.q)
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib().fm_host_free(self.ptr)
+            self.ptr = None
+
+
+def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_rows=None, roots=None,
+          profile=False, stream=None, allow_truncation=False):
+    """Run fm_match.  Returns the Result struct; with ``host_rows`` (a
+    PinnedRows or a C-contiguous uint32 numpy array) the table is copied there."""
+    o = MatchOpts()
+    lib().fm_match_opts_default(ctypes.byref(o))
+    o.mode = mode
+    o.columns = columns
+    o.profile = 1 if profile else 0
+    if stream is not None:
+        o.stream = stream
+    if roots is not None:
+        o.root_begin, o.root_end = int(roots[0]), int(roots[1])
+    if host_rows is not None:
+        if isinstance(host_rows, PinnedRows):
+            o.host_rows, o.host_rows_cap = host_rows.ptr, host_rows.cap
+        else:
+            assert host_rows.dtype == np.uint32 and host_rows.flags["C_CONTIGUOUS"]
+            o.host_rows = host_rows.ctypes.data
+            o.host_rows_cap = host_rows.size // max(1, query.q)
+    r = Result()
+    st = lib().fm_match(ctx._h, graph._h, query._h, ctypes.byref(o), ctypes.byref(r))
+    _check(st, "fm_match", allow=(FM_ERR_OUTPUT_OVERFLOW,) if allow_truncation else ())
+    return r
+
+
+def match_table(ctx, graph, query, columns=COLUMNS_REFERENCE, max_rows=1 << 24):
+    """Count and the table as a numpy array (rows copied to host)."""
+    q = query.q
+    buf = np.zeros(max_rows * q, dtype=np.uint32)
+    r = match(ctx, graph, query, mode=MODE_TABLE, columns=columns, host_rows=buf)
+    return r.count, buf[: r.rows_copied * q].reshape(-1, q), r

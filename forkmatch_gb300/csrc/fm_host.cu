@@ -1,0 +1,578 @@
+// fm_host.cu -- C ABI of libforkmatch: contexts, graphs, queries, matching.
+//
+// The matching driver replaces the reference's host match() (src/smsm.cu:1182-1349)
+// and its device-side fork machinery (src/smsm.cu:564-687, 949-1139: CDP child
+// launches on bank overflow, tail-launched bank frees).  Here the host walks
+// the levels depth first: it launches one expansion kernel per level, reads a
+// 64-byte control block back, and when a level's buffer filled it first drains
+// the deeper levels and then relaunches the level on the chunks that were
+// deferred.  Memory is therefore bounded by SOLN_PREALLOC (one buffer per
+// depth) and no device code waits on anything.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "fm_internal.h"
+
+namespace fm {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+fm_status cuda_fail(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return FM_ERR_CUDA;
+}
+
+}  // namespace fm
+
+using namespace fm;
+
+// ------------------------------------------------------------------ context
+
+struct fm_context {
+    fm_knobs knobs{};
+    int device = 0;
+    int sms = 1;
+    cudaStream_t stream = nullptr;
+    char* slab = nullptr;
+    uint64_t soln_bytes = 0, output_bytes = 0;
+    char* soln = nullptr;       // partial-match levels
+    uint32_t* output = nullptr; // embedding table
+    LaunchCtl* ctl = nullptr;   // device
+    MatchTotals* tot = nullptr; // device
+    uint32_t* defs = nullptr;   // 2 deferred lists per depth
+    uint32_t def_cap = 0;
+    LaunchCtl* h_ctl = nullptr; // pinned mirrors
+    MatchTotals* h_tot = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> prof;
+};
+
+namespace {
+
+uint64_t env_u64(const char* name, uint64_t dflt) {
+    const char* v = std::getenv(name);
+    if (!v || !*v) return dflt;
+    char* end = nullptr;
+    unsigned long long x = std::strtoull(v, &end, 10);
+    return (end && *end == 0) ? (uint64_t)x : dflt;
+}
+
+constexpr uint64_t kMiscBytes = 8ull << 20;
+
+}  // namespace
+
+extern "C" {
+
+const char* fm_status_string(fm_status s) {
+    switch (s) {
+        case FM_OK: return "ok";
+        case FM_ERR_ARG: return "invalid argument";
+        case FM_ERR_IO: return "file missing or unreadable";
+        case FM_ERR_DATA_HEADER0: return "data graph: missing \"t # 0\"";
+        case FM_ERR_DATA_TRAILER: return "data graph: missing \"t # -1\"";
+        case FM_ERR_DATA_HEADER: return "data graph: malformed header";
+        case FM_ERR_DATA_LINE: return "data graph: malformed line";
+        case FM_ERR_QUERY_FORMAT: return "query: malformed";
+        case FM_ERR_QUERY_MISSING: return "query: missing vertex or edge lines";
+        case FM_ERR_DISCONNECTED: return "query: disconnected or not plannable";
+        case FM_ERR_UNSUPPORTED: return "unsupported";
+        case FM_ERR_POOL: return "SOLN_PREALLOC too small";
+        case FM_ERR_OUTPUT_OVERFLOW: return "embedding table truncated at OUTPUT_PREALLOC";
+        case FM_ERR_CUDA: return "CUDA error";
+        case FM_ERR_DEVICE: return "device status error";
+        case FM_ERR_NOMEM: return "out of memory";
+    }
+    return "unknown";
+}
+
+const char* fm_last_error(void) { return g_last_error.c_str(); }
+
+const char* fm_version(void) { return "forkmatch-gb300 0.1 (sm_103a)"; }
+
+int fm_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+void fm_knobs_default(fm_knobs* k) {
+    // The reference's defaults (src/environment.cuh:4-6,17) were sized for a
+    // 48 GB RTX 8000; GB300 keeps the same proportions with room for a
+    // resident graph beside the slab.
+    k->prealloc_bytes = env_u64("FM_PREALLOC", 48ull << 30);
+    k->soln_prealloc_bytes = env_u64("FM_SOLN_PREALLOC", 24ull << 30);
+    k->output_prealloc_bytes = env_u64("FM_OUTPUT_PREALLOC", 18ull << 30);
+    k->bank_rows = (uint32_t)env_u64("FM_CUR_BANK_SIZE", 1u << 20);
+    k->device = (int32_t)env_u64("FM_DEVICE", 0);
+}
+
+void fm_match_opts_default(fm_match_opts* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->mode = FM_MODE_TABLE;
+    o->columns = FM_COLUMNS_REFERENCE;
+}
+
+void* fm_host_alloc(uint64_t bytes) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void fm_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+void fm_context_destroy(fm_context* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto e : c->prof) cudaEventDestroy(e);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->h_ctl) cudaFreeHost(c->h_ctl);
+    if (c->h_tot) cudaFreeHost(c->h_tot);
+    if (c->slab) cudaFree(c->slab);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+fm_status fm_context_create(const fm_knobs* knobs, fm_context** out) {
+    if (!out) return FM_ERR_ARG;
+    *out = nullptr;
+    fm_knobs k;
+    if (knobs) k = *knobs;
+    else fm_knobs_default(&k);
+    if (k.bank_rows == 0) k.bank_rows = 1;
+    uint64_t need = k.soln_prealloc_bytes + k.output_prealloc_bytes + kMiscBytes;
+    if (k.prealloc_bytes < need) {
+        set_error("PREALLOC must cover SOLN_PREALLOC + OUTPUT_PREALLOC + 8 MiB");
+        return FM_ERR_ARG;
+    }
+    std::unique_ptr<fm_context, void (*)(fm_context*)> c(new fm_context(), fm_context_destroy);
+    c->knobs = k;
+    c->device = k.device;
+    FM_CUDA(cudaSetDevice(c->device));
+    FM_CUDA(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device));
+    FM_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    cudaError_t e = cudaMalloc(&c->slab, k.prealloc_bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("cannot allocate PREALLOC bytes on the device");
+        return FM_ERR_NOMEM;
+    }
+    c->soln_bytes = k.soln_prealloc_bytes;
+    c->output_bytes = k.output_prealloc_bytes;
+    c->soln = c->slab;
+    c->output = (uint32_t*)(c->slab + ((k.soln_prealloc_bytes + 255) & ~255ull));
+    char* misc = c->slab + k.prealloc_bytes - kMiscBytes;
+    c->ctl = (LaunchCtl*)misc;
+    c->tot = (MatchTotals*)(misc + 256);
+    c->defs = (uint32_t*)(misc + 4096);
+    c->def_cap = (uint32_t)((kMiscBytes - 4096) / 4 / (2 * kMaxQ));
+    FM_CUDA(cudaHostAlloc(&c->h_ctl, sizeof(LaunchCtl), cudaHostAllocDefault));
+    FM_CUDA(cudaHostAlloc(&c->h_tot, sizeof(MatchTotals), cudaHostAllocDefault));
+    FM_CUDA(cudaEventCreate(&c->ev0));
+    FM_CUDA(cudaEventCreate(&c->ev1));
+    *out = c.release();
+    return FM_OK;
+}
+
+void* fm_context_stream(fm_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+// ------------------------------------------------------------------ graphs
+
+static void free_device_graph(DeviceGraph& g) {
+    if (g.seg) cudaFree(g.seg);
+    if (g.nbr) cudaFree(g.nbr);
+    g.seg = nullptr;
+    g.nbr = nullptr;
+}
+
+void fm_graph_free(fm_graph* g) {
+    if (!g) return;
+    cudaSetDevice(g->g.device);
+    free_device_graph(g->g);
+    delete g;
+}
+
+static fm_status graph_from_host_arrays(fm_context* ctx, uint32_t V, uint32_t L, uint64_t E, const uint32_t* src,
+                                        const uint32_t* dst, const uint32_t* lab, fm_graph** out) {
+    FM_CUDA(cudaSetDevice(ctx->device));
+    uint32_t* d = nullptr;
+    if (E) {
+        cudaError_t e = cudaMalloc(&d, E * 12);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            set_error("cannot allocate edge staging buffers");
+            return FM_ERR_NOMEM;
+        }
+        FM_CUDA(cudaMemcpyAsync(d, src, E * 4, cudaMemcpyHostToDevice, ctx->stream));
+        FM_CUDA(cudaMemcpyAsync(d + E, dst, E * 4, cudaMemcpyHostToDevice, ctx->stream));
+        FM_CUDA(cudaMemcpyAsync(d + 2 * E, lab, E * 4, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    std::unique_ptr<fm_graph> g(new fm_graph());
+    fm_status st = build_device_graph(g->g, V, L, E, d, d + E, d + 2 * E, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    if (d) cudaFree(d);
+    if (st != FM_OK) {
+        free_device_graph(g->g);
+        return st;
+    }
+    *out = g.release();
+    return FM_OK;
+}
+
+fm_status fm_graph_from_edges(fm_context* ctx, uint32_t vertices, uint32_t label_slots, uint64_t edges,
+                              const uint32_t* src, const uint32_t* dst, const uint32_t* label, fm_graph** out) {
+    if (!ctx || !out || (edges && (!src || !dst || !label))) return FM_ERR_ARG;
+    *out = nullptr;
+    if (label_slots > FM_MAX_LABEL + 1) {
+        set_error("label_slots above 256 (query labels are 8-bit)");
+        return FM_ERR_UNSUPPORTED;
+    }
+    return graph_from_host_arrays(ctx, vertices, label_slots, edges, src, dst, label, out);
+}
+
+fm_status fm_graph_load_text(fm_context* ctx, const char* text, uint64_t len, fm_graph** out) {
+    if (!ctx || !out || (!text && len)) return FM_ERR_ARG;
+    *out = nullptr;
+    EdgeArrays ea;
+    fm_status st = parse_data_text(text, len, ea);
+    if (st != FM_OK) return st;
+    return graph_from_host_arrays(ctx, ea.V, ea.L, ea.src.size(), ea.src.data(), ea.dst.data(), ea.lab.data(), out);
+}
+
+static bool read_file(const char* path, std::string& buf) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    f.seekg(0, std::ios::end);
+    std::streamoff n = f.tellg();
+    if (n < 0) return false;
+    f.seekg(0, std::ios::beg);
+    buf.resize((size_t)n);
+    if (n && !f.read(&buf[0], n)) return false;
+    return true;
+}
+
+fm_status fm_graph_load_file(fm_context* ctx, const char* path, fm_graph** out) {
+    if (!ctx || !path || !out) return FM_ERR_ARG;
+    *out = nullptr;
+    std::string buf;
+    if (!read_file(path, buf)) {
+        set_error(std::string("missing file ") + path);
+        return FM_ERR_IO;
+    }
+    return fm_graph_load_text(ctx, buf.data(), buf.size(), out);
+}
+
+fm_status fm_graph_get_info(const fm_graph* g, fm_graph_info* info) {
+    if (!g || !info) return FM_ERR_ARG;
+    const DeviceGraph& d = g->g;
+    info->vertices = d.V;
+    info->label_slots = d.L;
+    info->edges = d.E;
+    info->segments = d.segments;
+    info->long_segments = d.long_segments;
+    info->nbr_words = d.nbr_words;
+    info->max_list = d.max_len;
+    info->has_duplicates = d.has_dups;
+    info->device_bytes = (uint64_t)d.L * d.V * 16 + d.nbr_words * 4;
+    info->build_ms = d.build_ms;
+    return FM_OK;
+}
+
+// ------------------------------------------------------------------ queries
+
+fm_status fm_query_compile_text(const char* text, uint64_t len, fm_query** out) {
+    if (!out || (!text && len)) return FM_ERR_ARG;
+    *out = nullptr;
+    std::unique_ptr<fm_query> q(new fm_query());
+    fm_status st = compile_query_text(text, len, q->p);
+    if (st != FM_OK) return st;
+    *out = q.release();
+    return FM_OK;
+}
+
+fm_status fm_query_compile_file(const char* path, fm_query** out) {
+    if (!path || !out) return FM_ERR_ARG;
+    *out = nullptr;
+    std::string buf;
+    if (!read_file(path, buf)) {
+        set_error(std::string("missing file ") + path);
+        return FM_ERR_IO;
+    }
+    return fm_query_compile_text(buf.data(), buf.size(), out);
+}
+
+fm_status fm_query_get_info(const fm_query* q, fm_query_info* info) {
+    if (!q || !info) return FM_ERR_ARG;
+    std::memset(info, 0, sizeof(*info));
+    const Plan& p = q->p;
+    info->q = p.q;
+    info->e_lines = p.e_lines;
+    info->max_valency = p.max_valency;
+    for (uint32_t d = 0; d < p.q; d++) {
+        info->order[d] = p.inv[p.order_local[d]];
+        info->local_of_depth[d] = p.order_local[d];
+        info->inv[d] = p.inv[d];
+        info->nreq[d] = p.nreq[d];
+        info->pk_dist[d] = p.pk_dist[d];
+        for (uint32_t i = 0; i < p.nreq[d]; i++) {
+            info->req_climb[d][i] = p.req_climb[d][i];
+            info->req_label[d][i] = p.req_label[d][i];
+            info->req_refl[d][i] = p.req_refl[d][i];
+        }
+    }
+    info->automorphisms = p.automorphisms;
+    return FM_OK;
+}
+
+void fm_query_free(fm_query* q) { delete q; }
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ matching
+
+namespace {
+
+struct MatchRun {
+    fm_context* ctx;
+    const DeviceGraph* g;
+    const Plan* plan;
+    ExpandParams base;
+    cudaStream_t s;
+    bool table;
+    bool dups;
+    uint64_t level_cap;              // rows per level buffer
+    uint32_t* level[kMaxQ];          // SoA buffers, rows with d entries at level[d]
+    fm_result* res;
+    bool profile;
+    size_t prof_used = 0;
+    int block = 256;
+
+    fm_status launch_level(uint32_t d, uint64_t n_parents, bool roots) {
+        const uint32_t q = plan->q;
+        const int mode = (d == q - 1) ? (table ? kModeLastTable : kModeLastCount) : kModeMid;
+        const uint64_t n_chunks = (n_parents + 31) / 32;
+        uint32_t* def_a = ctx->defs + (size_t)(2 * d) * ctx->def_cap;
+        uint32_t* def_b = def_a + ctx->def_cap;
+        uint32_t ndef_in = 0;
+        uint64_t fresh = 0;
+        const size_t smem = expand_smem_bytes(d, plan->nreq[d], block / 32);
+        const int per_sm = expand_blocks_per_sm(mode, roots, dups, smem, block);
+        while (true) {
+            const uint64_t items = ndef_in + (n_chunks - fresh);
+            if (items == 0) break;
+            ExpandParams p = base;
+            p.pin = roots ? nullptr : level[d];
+            p.pstride = level_cap;
+            p.n_parents = n_parents;
+            p.depth = d;
+            p.def_in = def_a;
+            p.ndef_in = ndef_in;
+            p.fresh_base = fresh;
+            p.n_items = items;
+            p.def_out = def_b;
+            p.def_cap = ctx->def_cap;
+            p.pout = (mode == kModeMid) ? level[d + 1] : nullptr;
+            p.ocap = level_cap;
+            uint64_t want = (items + (block / 32) - 1) / (block / 32);
+            int grid = (int)std::min<uint64_t>(want, (uint64_t)ctx->sms * per_sm);
+            if (grid < 1) grid = 1;
+            FM_CUDA(cudaMemsetAsync(ctx->ctl, 0, sizeof(LaunchCtl), s));
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (profile) {
+                while (ctx->prof.size() < prof_used + 2) {
+                    cudaEvent_t e;
+                    FM_CUDA(cudaEventCreate(&e));
+                    ctx->prof.push_back(e);
+                }
+                e0 = ctx->prof[prof_used];
+                e1 = ctx->prof[prof_used + 1];
+                FM_CUDA(cudaEventRecord(e0, s));
+            }
+            FM_CUDA(launch_expand(p, mode, roots, dups, grid, block, smem, s));
+            if (profile) FM_CUDA(cudaEventRecord(e1, s));
+            FM_CUDA(cudaMemcpyAsync(ctx->h_ctl, ctx->ctl, sizeof(LaunchCtl), cudaMemcpyDeviceToHost, s));
+            FM_CUDA(cudaStreamSynchronize(s));
+            const LaunchCtl c = *ctx->h_ctl;
+            fm_level_stats& ls = res->level[d];
+            if (profile) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ls.kernel_ms += ms;
+            }
+            ls.launches++;
+            res->launches++;
+            ls.parents += c.parents;
+            ls.lookups += c.lookups;
+            ls.list_words += c.list_words;
+            if (c.error) {
+                set_error("deferred-chunk list overflow");
+                return FM_ERR_DEVICE;
+            }
+            const uint64_t claimed = std::min<uint64_t>(c.claim, items);
+            const uint64_t fresh_claimed = claimed > ndef_in ? claimed - ndef_in : 0;
+            const uint64_t carry = ndef_in > claimed ? ndef_in - claimed : 0;
+            fresh += fresh_claimed;
+            uint64_t ndef_out = c.ndef;
+            if (ndef_out + carry > ctx->def_cap) {
+                set_error("deferred-chunk list overflow");
+                return FM_ERR_DEVICE;
+            }
+            if (carry) {
+                FM_CUDA(cudaMemcpyAsync(def_b + ndef_out, def_a + claimed, carry * 4, cudaMemcpyDeviceToDevice, s));
+                ndef_out += carry;
+            }
+            if (mode == kModeMid) {
+                ls.produced += c.produced;
+                const uint64_t done_chunks = claimed - c.ndef;
+                if (done_chunks == 0 && c.produced == 0 && ndef_out == items) {
+                    set_error("one 32-parent chunk needs more rows than a level buffer holds; raise SOLN_PREALLOC");
+                    return FM_ERR_POOL;
+                }
+                if (c.produced) {
+                    fm_status st = launch_level(d + 1, c.produced, false);
+                    if (st != FM_OK) return st;
+                }
+            }
+            std::swap(def_a, def_b);
+            ndef_in = (uint32_t)ndef_out;
+        }
+        return FM_OK;
+    }
+};
+
+__global__ void k_iota_rows(uint32_t* out, uint64_t n, uint32_t first, uint64_t cap) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n && i < cap; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = first + (uint32_t)i;
+}
+
+}  // namespace
+
+extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_query* query,
+                              const fm_match_opts* opts_in, fm_result* out) {
+    if (!ctx || !graph || !query || !out) return FM_ERR_ARG;
+    fm_match_opts opts;
+    if (opts_in) opts = *opts_in;
+    else fm_match_opts_default(&opts);
+    std::memset(out, 0, sizeof(*out));
+    const DeviceGraph& g = graph->g;
+    const Plan& pl = query->p;
+    if (g.device != ctx->device) {
+        set_error("graph and context live on different devices");
+        return FM_ERR_ARG;
+    }
+    FM_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = opts.stream ? (cudaStream_t)opts.stream : ctx->stream;
+    const uint32_t q = pl.q;
+    out->q = q;
+    uint32_t rb = opts.root_begin, re = opts.root_end ? opts.root_end : g.V;
+    if (re > g.V) re = g.V;
+    if (rb > re) rb = re;
+    const bool table = opts.mode == FM_MODE_TABLE;
+    const uint64_t table_cap = ctx->output_bytes / (4ull * q);
+
+    // device plan
+    MatchRun run;
+    std::memset(&run.base, 0, sizeof(run.base));
+    DevPlan& dp = run.base.plan;
+    dp.q = q;
+    uint32_t r = 0;
+    bool impossible = false;
+    for (uint32_t d = 0; d < q; d++) {
+        dp.nreq[d] = pl.nreq[d];
+        dp.req_begin[d] = r;
+        for (uint32_t i = 0; i < pl.nreq[d]; i++, r++) {
+            dp.req_anc[r] = (uint8_t)(d - pl.req_climb[d][i]);
+            dp.req_label[r] = (uint8_t)pl.req_label[d][i];
+            if (pl.req_label[d][i] >= g.L) impossible = true;   // label absent from the data graph
+        }
+        dp.out_col[d] = (uint8_t)(opts.columns == FM_COLUMNS_QUERY_ID ? pl.inv[pl.order_local[d]] : q - 1 - d);
+    }
+    if ((uint64_t)g.max_len * 32 >= (1ull << 32)) {
+        set_error("a neighbour list is longer than 2^27");
+        return FM_ERR_UNSUPPORTED;
+    }
+
+    FM_CUDA(cudaMemsetAsync(ctx->tot, 0, sizeof(MatchTotals), s));
+    FM_CUDA(cudaEventRecord(ctx->ev0, s));
+    if (q == 1) {
+        uint64_t n = re - rb;
+        if (table && n) {
+            k_iota_rows<<<(unsigned)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(ctx->output, n, rb, table_cap);
+            FM_CUDA(cudaGetLastError());
+        }
+        out->count = n;
+    } else if (!impossible && re > rb) {
+        uint64_t sum_cols = 0;
+        for (uint32_t d = 2; d < q; d++) sum_cols += d;
+        uint64_t cap = sum_cols ? ctx->soln_bytes / (4ull * sum_cols) : 0;
+        const uint64_t bank = ctx->knobs.bank_rows;
+        if (sum_cols) {
+            cap = cap / bank * bank;
+            if (cap < (uint64_t)g.max_len * 32 + 32 || cap == 0) {
+                set_error("SOLN_PREALLOC cannot hold one 32-parent chunk per level for this graph");
+                return FM_ERR_POOL;
+            }
+        }
+        run.ctx = ctx;
+        run.g = &g;
+        run.plan = &pl;
+        run.s = s;
+        run.table = table;
+        run.dups = g.has_dups != 0;
+        run.level_cap = cap;
+        run.res = out;
+        run.profile = opts.profile != 0;
+        uint64_t off = 0;
+        for (uint32_t d = 0; d < kMaxQ; d++) run.level[d] = nullptr;
+        for (uint32_t d = 2; d < q; d++) {
+            run.level[d] = (uint32_t*)(ctx->soln + off);
+            off += 4ull * d * cap;
+        }
+        ExpandParams& b = run.base;
+        b.seg = g.seg;
+        b.nbr = g.nbr;
+        b.V = g.V;
+        b.root_begin = rb;
+        b.table = ctx->output;
+        b.table_cap = table_cap;
+        b.ctl = ctx->ctl;
+        b.tot = ctx->tot;
+        fm_status st = run.launch_level(1, re - rb, true);
+        if (st != FM_OK) return st;
+    }
+    FM_CUDA(cudaEventRecord(ctx->ev1, s));
+    FM_CUDA(cudaMemcpyAsync(ctx->h_tot, ctx->tot, sizeof(MatchTotals), cudaMemcpyDeviceToHost, s));
+    FM_CUDA(cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    out->device_ms = ms;
+    if (q > 1) out->count = table ? ctx->h_tot->table_pos : ctx->h_tot->count;
+    out->rows = table ? std::min<uint64_t>(out->count, table_cap) : 0;
+    out->truncated = table && out->count > table_cap;
+    out->rows_device = table ? ctx->output : nullptr;
+    if (q > 1) out->level[q - 1].produced = out->count;
+    if (table && opts.host_rows && out->rows) {
+        uint64_t n = std::min<uint64_t>(out->rows, opts.host_rows_cap);
+        FM_CUDA(cudaMemcpyAsync(opts.host_rows, ctx->output, n * q * 4, cudaMemcpyDeviceToHost, s));
+        FM_CUDA(cudaStreamSynchronize(s));
+        out->rows_copied = n;
+    }
+    out->h2d_bytes = out->launches * sizeof(ExpandParams);
+    out->d2h_bytes = out->launches * sizeof(LaunchCtl) + sizeof(MatchTotals) + out->rows_copied * q * 4;
+    if (out->truncated) {
+        set_error("embedding table truncated at OUTPUT_PREALLOC; count is exact");
+        return FM_ERR_OUTPUT_OVERFLOW;
+    }
+    return FM_OK;
+}

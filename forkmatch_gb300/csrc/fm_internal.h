@@ -1,0 +1,150 @@
+// fm_internal.h -- shared internals of libforkmatch (host + device).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "forkmatch.h"
+
+namespace fm {
+
+constexpr int kMaxQ = FM_MAX_QUERY_VERTICES;
+constexpr int kMaxReqTotal = 512;       // back edges over all depths of one query
+constexpr uint32_t kNoVertex = 0xffffffffu;
+
+// Thread-local error text (fm_last_error).
+void set_error(const std::string& msg);
+fm_status cuda_fail(cudaError_t e, const char* what);
+
+#define FM_CUDA(call)                                              \
+    do {                                                           \
+        cudaError_t _e = (call);                                   \
+        if (_e != cudaSuccess) return ::fm::cuda_fail(_e, #call); \
+    } while (0)
+
+// ----------------------------------------------------------------- data graph
+// Segment record of one (label, vertex) list, one 16-byte load per lookup:
+//   len <= 3 : {len, n0, n1, n2}      neighbours inline, unused slots 0xffffffff
+//   len >  3 : {len, off16, min, max} list at nbr[off16*4 .. off16*4+len), 16-B aligned
+struct DeviceGraph {
+    uint32_t V = 0;
+    uint32_t L = 0;            // label slots
+    uint32_t vbits = 0;        // bits per vertex id in the sort key
+    uint64_t E = 0;
+    uint4* seg = nullptr;      // L*V records, index label*V + v
+    uint32_t* nbr = nullptr;   // out-of-line lists
+    uint64_t nbr_words = 0;
+    uint64_t segments = 0, long_segments = 0;
+    uint32_t max_len = 0;
+    int has_dups = 0;
+    int device = 0;
+    double build_ms = 0;
+};
+
+// ----------------------------------------------------------------- query plan
+struct Plan {
+    uint32_t q = 0;
+    uint32_t e_lines = 0;
+    uint32_t max_valency = 0;
+    uint32_t inv[kMaxQ] = {};            // local -> original id
+    uint32_t order_local[kMaxQ] = {};    // depth -> local index
+    uint32_t nreq[kMaxQ] = {};
+    uint32_t req_climb[kMaxQ][kMaxQ] = {};
+    uint32_t req_label[kMaxQ][kMaxQ] = {};
+    uint32_t req_refl[kMaxQ][kMaxQ] = {};
+    uint32_t pk_dist[kMaxQ] = {};
+    uint64_t automorphisms = 0;
+};
+
+// Device-side copy of a plan, passed by value to every expansion launch.
+struct DevPlan {
+    uint32_t q;
+    uint32_t nreq[kMaxQ];
+    uint32_t req_begin[kMaxQ];
+    uint8_t req_anc[kMaxReqTotal];     // ancestor depth (row column) of each requirement
+    uint8_t req_label[kMaxReqTotal];
+    uint8_t out_col[kMaxQ];            // table column of the vertex matched at depth d
+};
+
+// Per-launch control block in device memory.
+struct LaunchCtl {
+    unsigned long long claim;       // work items claimed
+    unsigned long long budget;      // output rows reserved (upper bound)
+    unsigned long long produced;    // output rows written (exact)
+    unsigned long long parents;
+    unsigned long long lookups;
+    unsigned long long list_words;
+    unsigned int stop;              // level buffer full: stop claiming
+    unsigned int ndef;              // deferred chunks written
+    unsigned int error;
+    unsigned int pad;
+};
+
+// Per-match totals in device memory.
+struct MatchTotals {
+    unsigned long long count;       // embeddings (last level)
+    unsigned long long table_pos;   // rows reserved in the table
+    unsigned int error;
+    unsigned int pad[3];
+};
+
+enum KernelMode { kModeMid = 0, kModeLastTable = 1, kModeLastCount = 2 };
+
+struct ExpandParams {
+    DevPlan plan;
+    // graph
+    const uint4* seg;
+    const uint32_t* nbr;
+    uint32_t V;
+    // parents
+    const uint32_t* pin;            // SoA: column c at pin + c*pstride (null for roots)
+    uint64_t pstride;
+    uint64_t n_parents;
+    uint32_t root_begin;            // roots: parent p is vertex root_begin + p
+    uint32_t depth;                 // parent rows have `depth` entries; new vertex goes to column depth
+    // work items
+    const uint32_t* def_in;
+    uint32_t ndef_in;
+    uint64_t fresh_base;            // first fresh chunk
+    uint64_t n_items;               // ndef_in + fresh chunks
+    uint32_t* def_out;
+    uint32_t def_cap;
+    // outputs
+    uint32_t* pout;                 // SoA, column c at pout + c*ocap
+    uint64_t ocap;
+    uint32_t* table;                // rows of q
+    uint64_t table_cap;
+    LaunchCtl* ctl;
+    MatchTotals* tot;
+};
+
+// Launch one expansion kernel (fm_match.cu).
+cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups, int grid, int block,
+                          size_t smem, cudaStream_t s);
+size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps);
+int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block);
+
+// Device graph build from device edge arrays (fm_graph.cu).
+fm_status build_device_graph(DeviceGraph& g, uint32_t V, uint32_t L, uint64_t E, const uint32_t* d_src,
+                             const uint32_t* d_dst, const uint32_t* d_lab, cudaStream_t s);
+
+// Host parsers (fm_parse.cpp).
+struct EdgeArrays {
+    uint32_t V = 0, L = 0;
+    std::vector<uint32_t> src, dst, lab;
+};
+fm_status parse_data_text(const char* text, uint64_t len, EdgeArrays& out);
+fm_status compile_query_text(const char* text, uint64_t len, Plan& out);
+
+}  // namespace fm
+
+struct fm_graph {
+    fm::DeviceGraph g;
+};
+
+struct fm_query {
+    fm::Plan p;
+};

@@ -1,0 +1,271 @@
+// fm_match.cu -- level-expansion kernel of the matcher.
+//
+// Replaces the reference's per-thread k-way merge (src/smsm.cu:299-345 isoGen,
+// src/smsm.cu:57-140 isoCompare), injectivity walk (src/smsm.cu:188-227 isInj),
+// ballot append (src/smsm.cu:146-182 attemptInsert) and table write
+// (src/smsm.cu:706-779 isoWrite).
+//
+// One launch extends a level of partial matches by one query vertex.  Partial
+// matches are full rows (column c = data vertex matched at depth c) stored
+// column-major (SoA) so every load and store of a column is coalesced; there is
+// no parent-pointer forest to climb.  A warp claims 32 parents at a time:
+//   1. each lane loads its parent row and the k (label, ancestor) segment
+//      records -- k independent 16-byte loads, issued back to back;
+//   2. the shortest list is the driver; a warp prefix sum over driver lengths
+//      turns the 32 parents' candidate lists into one range of slots;
+//   3. lanes take 32 consecutive slots per round (load-balanced across
+//      parents, so a hub parent keeps all 32 lanes busy), test membership of
+//      the driver value in the other k-1 lists (inline compare or binary
+//      search), reject values already in the row, and append survivors with
+//      one atomic per warp round (__ballot_sync + __popc rank).
+// Lists of length <= 3 are inline in the segment record, so the common case
+// needs no second memory access.  With duplicate e-lines the value at rank r of
+// its run in the driver list survives only if every other list holds at least
+// r + 1 copies (min-multiplicity semantics of the reference's merge).
+//
+// Bounded memory: before expanding, a warp reserves its candidate upper bound
+// in the output level ("budget"); when a reservation does not fit, the warp
+// records its chunk in a deferred list, raises `stop`, and exits; the host
+// drains the output level (depth first) and relaunches this level on the
+// deferred chunks plus the unclaimed remainder.  Nothing spins, nothing traps.
+#include "fm_internal.h"
+
+namespace fm {
+namespace {
+
+constexpr int kWarps = 8;
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ uint4 ldg4(const uint4* p) { return __ldg(p); }
+
+__device__ __forceinline__ uint32_t seg_at(const uint4& s, uint32_t t, const uint32_t* __restrict__ nbr) {
+    if (s.x <= 3) return t == 0 ? s.y : (t == 1 ? s.z : s.w);
+    return __ldg(nbr + (uint64_t)s.y * 4 + t);
+}
+
+// lower_bound of x in a[0, n)
+__device__ __forceinline__ uint32_t lower_bound_g(const uint32_t* __restrict__ a, uint32_t n, uint32_t x) {
+    uint32_t lo = 0;
+    while (n > 0) {
+        uint32_t half = n >> 1;
+        if (__ldg(a + lo + half) < x) {
+            lo += half + 1;
+            n -= half + 1;
+        } else {
+            n = half;
+        }
+    }
+    return lo;
+}
+
+// Does the list hold at least `need` copies of x?
+__device__ __forceinline__ bool seg_has(const uint4& s, uint32_t x, uint32_t need, const uint32_t* __restrict__ nbr) {
+    if (s.x <= 3) {
+        uint32_t c = (s.x > 0 && s.y == x) + (s.x > 1 && s.z == x) + (s.x > 2 && s.w == x);
+        return c >= need;
+    }
+    if (x < s.z || x > s.w) return false;
+    const uint32_t* a = nbr + (uint64_t)s.y * 4;
+    uint32_t pos = lower_bound_g(a, s.x, x) + need - 1;
+    return pos < s.x && __ldg(a + pos) == x;
+}
+
+// Rank of position t within its run of equal values.
+__device__ __forceinline__ uint32_t seg_rank(const uint4& s, uint32_t t, uint32_t x, const uint32_t* __restrict__ nbr) {
+    if (s.x <= 3) return (t >= 1 && s.y == x) + (t >= 2 && s.z == x);
+    const uint32_t* a = nbr + (uint64_t)s.y * 4;
+    return t - lower_bound_g(a, t, x);
+}
+
+__device__ __forceinline__ void defer_chunk(const ExpandParams& P, uint32_t chunk) {
+    unsigned idx = atomicAdd(&P.ctl->ndef, 1u);
+    if (idx < P.def_cap) P.def_out[idx] = chunk;
+    else atomicOr(&P.ctl->error, 1u);
+}
+
+template <int MODE, bool ROOTS, bool DUPS>
+__global__ void __launch_bounds__(kWarps * 32) k_expand(const __grid_constant__ ExpandParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t d = P.depth;
+    const uint32_t k = P.plan.nreq[d];
+    const uint32_t rb = P.plan.req_begin[d];
+    const uint32_t per_warp = 128 * d + 512 * k + 256;
+    unsigned char* ws = smem_raw + warp * per_warp;
+    uint32_t* rows_s = (uint32_t*)ws;                    // [d][32]
+    uint4* segs_s = (uint4*)(ws + 128 * d);              // [k][32]
+    uint32_t* excl_s = (uint32_t*)(ws + 128 * d + 512 * k);
+    uint32_t* drv_s = excl_s + 32;
+
+    unsigned long long n_count = 0, n_lookups = 0, n_words = 0, n_parents = 0;
+
+    for (;;) {
+        unsigned long long item = 0;
+        if (lane == 0) item = atomicAdd(&P.ctl->claim, 1ull);
+        item = __shfl_sync(kFull, item, 0);
+        if (item >= P.n_items) break;
+        const uint32_t chunk = item < P.ndef_in ? P.def_in[item] : (uint32_t)(P.fresh_base + (item - P.ndef_in));
+        if (MODE == kModeMid) {
+            if (*(volatile unsigned int*)&P.ctl->stop) {
+                if (lane == 0) defer_chunk(P, chunk);
+                break;
+            }
+        }
+        const uint64_t p = (uint64_t)chunk * 32 + lane;
+        const bool valid = p < P.n_parents;
+        if (ROOTS) {
+            rows_s[lane] = P.root_begin + (uint32_t)p;
+        } else {
+            for (uint32_t c = 0; c < d; c++) rows_s[c * 32 + lane] = valid ? P.pin[c * P.pstride + p] : 0u;
+        }
+        uint32_t n = 0, drv = 0;
+        unsigned long long w = 0;
+        if (valid) {
+            uint32_t best = 0xffffffffu;
+            for (uint32_t i = 0; i < k; i++) {
+                const uint32_t anc = P.plan.req_anc[rb + i];
+                const uint32_t lab = P.plan.req_label[rb + i];
+                const uint32_t v = rows_s[anc * 32 + lane];
+                const uint4 s = ldg4(P.seg + (uint64_t)lab * P.V + v);
+                segs_s[i * 32 + lane] = s;
+                w += s.x;
+                if (s.x < best) {
+                    best = s.x;
+                    drv = i;
+                }
+            }
+            n = best;
+        }
+        uint32_t incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(kFull, incl, o);
+            if ((int)lane >= o) incl += t;
+        }
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        if (MODE == kModeMid) {
+            int ok = 1;
+            if (lane == 0 && total) {
+                unsigned long long old = atomicAdd(&P.ctl->budget, (unsigned long long)total);
+                if (old + total > P.ocap) {
+                    ok = 0;
+                    atomicExch(&P.ctl->stop, 1u);
+                    defer_chunk(P, chunk);
+                }
+            }
+            ok = __shfl_sync(kFull, ok, 0);
+            if (!ok) break;
+        }
+        if (valid) {
+            n_lookups += k;
+            n_words += w;
+            n_parents += 1;
+        }
+        excl_s[lane] = incl - n;
+        drv_s[lane] = drv;
+        __syncwarp();
+        for (uint32_t base = 0; base < total; base += 32) {
+            const uint32_t s = base + lane;
+            bool ok = false;
+            uint32_t x = 0, j = 0;
+            if (s < total) {
+#pragma unroll
+                for (uint32_t step = 16; step; step >>= 1)
+                    if (excl_s[j + step] <= s) j += step;
+                const uint32_t t = s - excl_s[j];
+                const uint32_t dj = drv_s[j];
+                const uint4 ds = segs_s[dj * 32 + j];
+                x = seg_at(ds, t, P.nbr);
+                uint32_t need = 1;
+                if (DUPS) need = seg_rank(ds, t, x, P.nbr) + 1;
+                ok = true;
+                for (uint32_t i = 0; i < k && ok; i++) {
+                    if (i == dj) continue;
+                    ok = seg_has(segs_s[i * 32 + j], x, need, P.nbr);
+                }
+                for (uint32_t c = 0; c < d && ok; c++) ok = rows_s[c * 32 + j] != x;
+            }
+            const unsigned ball = __ballot_sync(kFull, ok);
+            const uint32_t cnt = __popc(ball);
+            if (MODE == kModeLastCount) {
+                n_count += cnt;
+            } else if (cnt) {
+                unsigned long long pos0 = 0;
+                if (lane == 0)
+                    pos0 = atomicAdd(MODE == kModeMid ? &P.ctl->produced : &P.tot->table_pos,
+                                     (unsigned long long)cnt);
+                pos0 = __shfl_sync(kFull, pos0, 0);
+                if (ok) {
+                    const uint64_t pos = pos0 + __popc(ball & ((1u << lane) - 1u));
+                    if (MODE == kModeMid) {
+                        for (uint32_t c = 0; c < d; c++) P.pout[c * P.ocap + pos] = rows_s[c * 32 + j];
+                        P.pout[d * P.ocap + pos] = x;
+                    } else if (pos < P.table_cap) {
+                        uint32_t* r = P.table + pos * P.plan.q;
+                        for (uint32_t c = 0; c < d; c++) r[P.plan.out_col[c]] = rows_s[c * 32 + j];
+                        r[P.plan.out_col[d]] = x;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
+    // commit statistics: one atomic per warp per counter
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        n_lookups += __shfl_down_sync(kFull, n_lookups, o);
+        n_words += __shfl_down_sync(kFull, n_words, o);
+        n_parents += __shfl_down_sync(kFull, n_parents, o);
+    }
+    if (lane == 0) {
+        if (n_parents) {
+            atomicAdd(&P.ctl->parents, n_parents);
+            atomicAdd(&P.ctl->lookups, n_lookups);
+            atomicAdd(&P.ctl->list_words, n_words);
+        }
+        if (MODE == kModeLastCount && n_count) atomicAdd(&P.tot->count, n_count);
+    }
+}
+
+template <int MODE, bool ROOTS, bool DUPS>
+void* kernel_ptr() {
+    return (void*)&k_expand<MODE, ROOTS, DUPS>;
+}
+
+void* pick(int mode, bool roots, bool dups) {
+#define FM_PICK(M)                                                                         \
+    if (mode == M) {                                                                       \
+        if (roots) return dups ? kernel_ptr<M, true, true>() : kernel_ptr<M, true, false>(); \
+        return dups ? kernel_ptr<M, false, true>() : kernel_ptr<M, false, false>();        \
+    }
+    FM_PICK(kModeMid)
+    FM_PICK(kModeLastTable)
+    FM_PICK(kModeLastCount)
+#undef FM_PICK
+    return nullptr;
+}
+
+}  // namespace
+
+size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps) {
+    return (size_t)warps * (128u * depth + 512u * nreq + 256u);
+}
+
+int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block) {
+    void* f = pick(mode, roots, dups);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, block, smem) != cudaSuccess || n < 1) n = 1;
+    return n;
+}
+
+cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups, int grid, int block,
+                          size_t smem, cudaStream_t s) {
+    void* f = pick(mode, roots, dups);
+    if (!f) return cudaErrorInvalidValue;
+    void* args[] = {(void*)&p};
+    return cudaLaunchKernel(f, dim3(grid), dim3(block), args, smem, s);
+}
+
+}  // namespace fm

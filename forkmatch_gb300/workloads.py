@@ -1,0 +1,51 @@
+"""Synthetic workloads with the shapes of the benchmark configurations.
+
+Every graph is generated from a fixed seed by ``forkmatch_gb300.synth``; the
+edge arrays are hashed so a run can tell whether its generator reproduced the
+recorded graph exactly.
+
+plain_at_scale (the headline workload):
+    R-MAT(a=0.57, b=0.19, c=0.19, d=0.05), 2^20 vertices, 16M distinct
+    undirected edges without self loops (32M directed e-lines), vertex labels
+    Zipf(s=1.2) over 4 values (ignored by matching, as in the reference), edge
+    labels uniform over 32 (written 1..32), uint32 ids.  16 queries of 8
+    vertices, matched one at a time with full uint32 embedding tables.
+    The query set is recorded in tests/golden/workload_plain_at_scale.json.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+
+from forkmatch_gb300 import synth as S
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+PLAIN_AT_SCALE = dict(scale=20, m=16_000_000, n_elabels=32, n_vlabels=4, seed=2, vlabel_seed=3)
+PLAIN_SMALL = dict(n=1000, m=2000, n_elabels=87, seed=1)
+
+
+def edge_hash(src, dst, lab):
+    h = hashlib.sha256()
+    for a in (src, dst, lab):
+        h.update(np.ascontiguousarray(a, dtype=np.uint32).tobytes())
+    return h.hexdigest()
+
+
+def plain_at_scale_graph():
+    p = PLAIN_AT_SCALE
+    rng = np.random.default_rng(p["vlabel_seed"])
+    vlab = S.zipf_labels(rng, 1 << p["scale"], p["n_vlabels"], s=1.2)
+    return S.rmat(p["scale"], p["m"], p["seed"], p["n_elabels"], vlab=vlab, n_vlabels=p["n_vlabels"])
+
+
+def plain_small_graph():
+    p = PLAIN_SMALL
+    return S.erdos_renyi(p["n"], p["m"], p["seed"], p["n_elabels"])
+
+
+def load_workload(name):
+    with open(os.path.join(GOLDEN, "workload_%s.json" % name)) as f:
+        return json.load(f)

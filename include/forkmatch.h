@@ -1,0 +1,202 @@
+/*
+ * forkmatch.h -- C ABI of libforkmatch, a GB300-native (sm_103a) edge-labelled
+ * subgraph-isomorphism matcher that is a drop-in for ForkMatch.
+ *
+ * The reference has no library or FFI: its API surface is the CLI
+ * `ForkMatch <query.g> <data.g>` (src/smsm.cu:1351-1393), the .g text format
+ * (README.md:5-27), the environment.cuh knobs (src/environment.cuh:4-20) and the
+ * embedding table it leaves in device memory (src/smsm.cu:706-779).  Each entry
+ * point below names the reference code it replaces.  Plain C types only: no
+ * CUDA or torch types appear in the signatures (streams are passed as void*).
+ *
+ * Semantics (identical to the reference): an embedding is an injective map f
+ * from query vertices to data vertices such that for every query e-line
+ * (x -> a, label l) with a matched before x, the data graph has an e-line
+ * (f(a) -> f(x)) with label l.  Vertex labels are ignored; matches are not
+ * induced; duplicate data e-lines yield duplicate embeddings (a value present
+ * in every intersected list is produced min(multiplicity) times).
+ */
+#ifndef FORKMATCH_H
+#define FORKMATCH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FM_MAX_QUERY_VERTICES 32
+#define FM_MAX_LABEL 255
+
+/* Status codes.  Replace the reference's exit()/__trap() error paths
+ * (src/trie.cuh:1059-1092, src/hostparser.cuh:15-18,292-387,
+ * src/ccsr.cuh:252-254,581-583,719-725, src/tbs.cuh:57-68, src/smsm.cu:898);
+ * the CLI maps them back to the reference's exit codes. */
+typedef enum fm_status {
+    FM_OK = 0,
+    FM_ERR_ARG = 1,             /* bad argument */
+    FM_ERR_IO = 2,              /* file missing/unreadable            (exit 12 / 232) */
+    FM_ERR_DATA_HEADER0 = 3,    /* data text does not start "t # 0\n" (exit 76) */
+    FM_ERR_DATA_TRAILER = 4,    /* data text does not end "t # -1"    (exit 77) */
+    FM_ERR_DATA_HEADER = 5,     /* malformed data header              (exit 78) */
+    FM_ERR_DATA_LINE = 6,       /* malformed/out-of-range data line   (reference traps) */
+    FM_ERR_QUERY_FORMAT = 7,    /* malformed query text               (exit 233) */
+    FM_ERR_QUERY_MISSING = 8,   /* fewer v/e lines than the header    (exit 234) */
+    FM_ERR_DISCONNECTED = 9,    /* query not traversable by the planner (exit 1) */
+    FM_ERR_UNSUPPORTED = 10,    /* query outside supported limits */
+    FM_ERR_POOL = 11,           /* SOLN_PREALLOC too small for one work chunk */
+    FM_ERR_OUTPUT_OVERFLOW = 12,/* table truncated at OUTPUT_PREALLOC (count stays exact) */
+    FM_ERR_CUDA = 13,           /* CUDA runtime error (fm_last_error() has the text) */
+    FM_ERR_DEVICE = 14,         /* device-side status word reported an error */
+    FM_ERR_NOMEM = 15           /* allocation failed */
+} fm_status;
+
+const char* fm_status_string(fm_status s);
+/* Text of the last error raised on the calling thread. */
+const char* fm_last_error(void);
+
+/* Knobs.  Same names and roles as src/environment.cuh:4-20:
+ *   PREALLOC       -> prealloc_bytes        (whole device slab of a context)
+ *   SOLN_PREALLOC  -> soln_prealloc_bytes   (partial-match levels)
+ *   OUTPUT_PREALLOC-> output_prealloc_bytes (embedding table)
+ *   CurBankSize    -> bank_rows             (level capacity granularity, rows)
+ * fm_knobs_default() gives GB300 defaults, overridden by the environment
+ * variables FM_PREALLOC, FM_SOLN_PREALLOC, FM_OUTPUT_PREALLOC, FM_CUR_BANK_SIZE
+ * (bytes / rows, decimal). */
+typedef struct fm_knobs {
+    uint64_t prealloc_bytes;
+    uint64_t soln_prealloc_bytes;
+    uint64_t output_prealloc_bytes;
+    uint32_t bank_rows;
+    int32_t device;
+} fm_knobs;
+
+void fm_knobs_default(fm_knobs* k);
+
+/* A context owns one device slab (prealloc) and one CUDA stream.  Replaces
+ * prealloc()/p_malloc (src/smsm.cu:1171-1180, src/trie.cuh:1029-1049). */
+typedef struct fm_context fm_context;
+fm_status fm_context_create(const fm_knobs* knobs, fm_context** out);
+void fm_context_destroy(fm_context* ctx);
+/* cudaStream_t of the context, as void*. */
+void* fm_context_stream(fm_context* ctx);
+
+/* Resident data graph: label-partitioned, 16-byte-aligned neighbour segments
+ * in device memory.  Replaces parseGraph/parseCSR/csrToTrie and
+ * BaseGPUGraph::neighbours (src/trie.cuh:1051-1222, 800-951, 750-795, 266-310).
+ * Graph memory is sized to fit at load time (not carved from the slab), so one
+ * resident graph serves every context on the same device. */
+typedef struct fm_graph fm_graph;
+typedef struct fm_graph_info {
+    uint32_t vertices;
+    uint32_t label_slots;       /* labels 0 .. label_slots-1 are indexable */
+    uint64_t edges;             /* directed e-lines kept */
+    uint64_t segments;          /* non-empty (label, vertex) lists */
+    uint64_t long_segments;     /* lists stored out of line (length > 3) */
+    uint64_t nbr_words;         /* u32 words of out-of-line storage (16 B aligned) */
+    uint32_t max_list;          /* longest (label, vertex) list */
+    int32_t has_duplicates;     /* some (label, src, dst) e-line occurs twice */
+    uint64_t device_bytes;      /* graph bytes resident on the device */
+    double build_ms;            /* device build time */
+} fm_graph_info;
+
+/* `.g` file / in-memory text (the reference parser's grammar, README.md:5-27). */
+fm_status fm_graph_load_file(fm_context* ctx, const char* path, fm_graph** out);
+fm_status fm_graph_load_text(fm_context* ctx, const char* text, uint64_t len, fm_graph** out);
+/* Directed e-lines from host arrays (both directions must be listed). */
+fm_status fm_graph_from_edges(fm_context* ctx, uint32_t vertices, uint32_t label_slots, uint64_t edges,
+                              const uint32_t* src, const uint32_t* dst, const uint32_t* label,
+                              fm_graph** out);
+fm_status fm_graph_get_info(const fm_graph* g, fm_graph_info* info);
+void fm_graph_free(fm_graph* g);
+
+/* Compiled query: the reference's matching order and per-depth requirements
+ * (src/hostparser.cuh:286-508 fileParse, src/ccsr.cuh:485-728 preProcessQuery,
+ * src/ccsr.cuh:229-326 genereateCCSRRequirements) plus its automorphism count
+ * (src/ccsr.cuh:383-465 queryMatch). */
+typedef struct fm_query fm_query;
+typedef struct fm_query_info {
+    uint32_t q;                                   /* query vertices */
+    uint32_t e_lines;                             /* query e-lines */
+    uint32_t max_valency;                         /* longest CCSR row */
+    uint32_t order[FM_MAX_QUERY_VERTICES];        /* original vertex id matched at depth d */
+    uint32_t local_of_depth[FM_MAX_QUERY_VERTICES];/* reference local (degree-sorted) index at depth d */
+    uint32_t inv[FM_MAX_QUERY_VERTICES];          /* reference invVertices: local -> original id */
+    uint32_t nreq[FM_MAX_QUERY_VERTICES];         /* back edges per depth */
+    uint32_t req_climb[FM_MAX_QUERY_VERTICES][FM_MAX_QUERY_VERTICES];
+    uint32_t req_label[FM_MAX_QUERY_VERTICES][FM_MAX_QUERY_VERTICES];
+    uint32_t req_refl[FM_MAX_QUERY_VERTICES][FM_MAX_QUERY_VERTICES];
+    uint32_t pk_dist[FM_MAX_QUERY_VERTICES];
+    uint64_t automorphisms;                       /* |Aut| (label-preserving), 0 if not computed */
+} fm_query_info;
+
+fm_status fm_query_compile_file(const char* path, fm_query** out);
+fm_status fm_query_compile_text(const char* text, uint64_t len, fm_query** out);
+fm_status fm_query_get_info(const fm_query* q, fm_query_info* info);
+void fm_query_free(fm_query* q);
+
+/* Matching.  Replaces initPosting/isoInit/isoLoop/isoMatch/isoGen/isInj/
+ * attemptInsert/isoWrite and the CDP fork machinery (src/smsm.cu:15-1166)
+ * and the host driver match() (src/smsm.cu:1182-1349). */
+typedef enum fm_mode {
+    FM_MODE_TABLE = 0,          /* count + embedding table (reference WriteSolnFlag = true) */
+    FM_MODE_COUNT = 1           /* count only */
+} fm_mode;
+
+typedef enum fm_columns {
+    FM_COLUMNS_REFERENCE = 0,   /* column i = vertex matched at depth q-1-i (src/smsm.cu:743-760) */
+    FM_COLUMNS_QUERY_ID = 1     /* column i = original query vertex i */
+} fm_columns;
+
+typedef struct fm_match_opts {
+    int32_t mode;               /* fm_mode */
+    int32_t columns;            /* fm_columns */
+    void* stream;               /* cudaStream_t to run on, or NULL for the context stream */
+    uint32_t* host_rows;        /* optional: copy the table here (host memory, pinned preferred) */
+    uint64_t host_rows_cap;     /* rows that fit in host_rows */
+    uint32_t root_begin;        /* roots (depth-0 images) in [root_begin, root_end); */
+    uint32_t root_end;          /*   root_end == 0 means all vertices */
+    int32_t profile;            /* 1: time every expansion launch with CUDA events */
+} fm_match_opts;
+
+void fm_match_opts_default(fm_match_opts* o);
+
+typedef struct fm_level_stats {
+    uint64_t parents;           /* partial matches expanded at this depth */
+    uint64_t lookups;           /* (vertex, label) list lookups */
+    uint64_t list_words;        /* sum of looked-up list lengths */
+    uint64_t produced;          /* partial matches (or embeddings) produced */
+    uint32_t launches;
+    double kernel_ms;           /* sum of launch durations (profile = 1) */
+} fm_level_stats;
+
+typedef struct fm_result {
+    uint64_t count;             /* exact number of embeddings (u64) */
+    uint64_t rows;              /* rows in the device table (min(count, capacity)) */
+    const uint32_t* rows_device;/* device table in the context slab; valid until the next match */
+    uint64_t rows_copied;       /* rows copied to opts.host_rows */
+    int32_t truncated;          /* table capacity exceeded */
+    uint32_t q;                 /* row width */
+    double device_ms;           /* matching window on the device (CUDA events) */
+    uint64_t launches;          /* expansion kernel launches */
+    uint64_t h2d_bytes;         /* host->device bytes this match moved (kernel parameter blocks) */
+    uint64_t d2h_bytes;         /* device->host bytes (control blocks, totals, copied rows) */
+    fm_level_stats level[FM_MAX_QUERY_VERTICES];
+} fm_result;
+
+fm_status fm_match(fm_context* ctx, const fm_graph* g, const fm_query* q,
+                   const fm_match_opts* opts, fm_result* out);
+
+/* Pinned host memory helpers (cudaHostAlloc / cudaFreeHost). */
+void* fm_host_alloc(uint64_t bytes);
+void fm_host_free(void* p);
+
+/* Library / device identification. */
+const char* fm_version(void);
+int fm_device_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,248 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Every test here runs the product kernels on the GPU and compares with the
+oracle (counts bit-exact, tables as sorted row sets, per-level work counters
+exact) or with closed-form counts.  Integer work: no tolerance anywhere."""
+import math
+
+import numpy as np
+import pytest
+
+import forkmatch_gb300 as fm
+from forkmatch_gb300 import synth as S
+from oracle import oracle as O
+from tests.helpers import complete_graph, cycle_graph, golden_graphs, star_graph
+
+pytestmark = pytest.mark.gpu
+
+GB = 1 << 30
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from forkmatch_gb300 import build
+    build.build()
+    c = fm.Context(prealloc_bytes=3 * GB, soln_prealloc_bytes=1 * GB, output_prealloc_bytes=1 * GB,
+                   bank_rows=1024)
+    yield c
+    c.close()
+
+
+def sorted_rows(a):
+    a = np.asarray(a, dtype=np.uint32)
+    if a.size == 0:
+        return a.reshape(0, 0)
+    idx = np.lexsort(a.T[::-1])
+    return a[idx]
+
+
+def check_case(ctx, g, og, qtext, expect_count=None, table=True, max_rows=1 << 20):
+    p = O.plan(qtext, enumerate_aut=0)
+    oc, orows, ost = O.match(og, p, table=table, table_cap=max_rows)
+    if expect_count is not None:
+        assert oc == expect_count
+    q = fm.Query.from_text(qtext)
+    r = fm.match(ctx, g, q, mode=fm.MODE_COUNT)
+    assert r.count == oc
+    for d in range(1, p.q):
+        assert r.level[d].lookups == ost.lookups[d], ("lookups", d)
+        assert r.level[d].list_words == ost.list_words[d], ("list_words", d)
+        assert r.level[d].parents == ost.partials[d - 1], ("parents", d)
+    if table and oc <= max_rows:
+        cnt, rows, r2 = fm.match_table(ctx, g, q, max_rows=max_rows)
+        assert cnt == oc
+        assert np.array_equal(sorted_rows(rows), sorted_rows(orows))
+    return oc
+
+
+def test_golden_cases_count_table_and_work_counters(ctx):
+    n = 0
+    for case, G, text in golden_graphs():
+        g = fm.Graph.from_text(ctx, text)
+        og = O.Graph.parse(text)
+        info = g.info()
+        assert info.edges == case["E"] and info.vertices == case["V"]
+        for e in case["cases"]:
+            c = check_case(ctx, g, og, e["text"].encode(), expect_count=e["count"])
+            n += 1
+            assert c == e["count"]
+    assert n > 50
+
+
+@pytest.mark.parametrize("n", [5, 9, 33])
+def test_complete_graph_closed_forms(ctx, n):
+    V, s, d, l = complete_graph(n)
+    g = fm.Graph.from_edges(ctx, V, 2, s, d, l)
+    for qq, want in [(S.query_cycle(3, [1] * 3), n * (n - 1) * (n - 2)),
+                     (S.query_cycle(4, [1] * 4), n * (n - 1) * (n - 2) * (n - 3)),
+                     (S.query_clique(4, [1]), math.perm(n, 4)),
+                     (S.query_clique(5, [1]), math.perm(n, 5))]:
+        r = fm.match(ctx, g, fm.Query.from_text(qq.to_g_text()), mode=fm.MODE_COUNT)
+        assert r.count == want
+
+
+def test_star_and_cycle_closed_forms(ctx):
+    V, s, d, l = star_graph(40)
+    g = fm.Graph.from_edges(ctx, V, 2, s, d, l)
+    for k in (2, 3, 4):
+        r = fm.match(ctx, g, fm.Query.from_text(S.query_star(k + 1, [1] * k).to_g_text()), mode=fm.MODE_COUNT)
+        assert r.count == math.perm(40, k)
+    V, s, d, l = cycle_graph(1000)
+    g = fm.Graph.from_edges(ctx, V, 2, s, d, l)
+    for k in (2, 5, 9):
+        r = fm.match(ctx, g, fm.Query.from_text(S.query_path(k, [1] * k).to_g_text()), mode=fm.MODE_COUNT)
+        assert r.count == 2000
+
+
+def test_label_mismatch_and_absent_label(ctx):
+    V, s, d, l = complete_graph(6, label=2)
+    g = fm.Graph.from_edges(ctx, V, 3, s, d, l)
+    assert fm.match(ctx, g, fm.Query.from_text(S.query_cycle(3, [1] * 3).to_g_text())).count == 0
+    # label 7 is beyond the graph's label slots: no embedding, no out-of-range lookup
+    assert fm.match(ctx, g, fm.Query.from_text(S.query_path(3, [7, 7]).to_g_text())).count == 0
+
+
+def test_duplicate_edges_min_multiplicity(ctx):
+    rng = np.random.default_rng(3)
+    V = 40
+    m = 400
+    src = rng.integers(0, V, m).astype(np.uint32)
+    dst = rng.integers(0, V, m).astype(np.uint32)
+    keep = src != dst
+    src, dst = src[keep], dst[keep]
+    lab = rng.integers(1, 3, len(src)).astype(np.uint32)
+    # both directions, then duplicate a third of the e-lines
+    S2 = np.concatenate([src, dst])
+    D2 = np.concatenate([dst, src])
+    L2 = np.concatenate([lab, lab])
+    dup = rng.random(len(S2)) < 0.33
+    S2 = np.concatenate([S2, S2[dup]])
+    D2 = np.concatenate([D2, D2[dup]])
+    L2 = np.concatenate([L2, L2[dup]])
+    g = fm.Graph.from_edges(ctx, V, 3, S2, D2, L2)
+    assert g.info().has_duplicates
+    og = O.Graph.from_edges(V, 3, S2, D2, L2)
+    for qq in [S.query_path(3, [1, 2]), S.query_cycle(3, [1, 1, 2]), S.query_cycle(4, [1, 2, 1, 2]),
+               S.query_clique(4, [1, 2]), S.query_star(4, [1, 1, 2])]:
+        check_case(ctx, g, og, qq.to_g_text())
+
+
+def test_rmat_random_walk_queries(ctx):
+    G = S.rmat(14, 60000, seed=11, n_elabels=6)
+    src, dst, lab = G.directed()
+    g = fm.Graph.from_edges(ctx, G.V, 7, src, dst, lab)
+    og = O.Graph.from_edges(G.V, 7, src, dst, lab)
+    rng = np.random.default_rng(12)
+    done = 0
+    for i in range(30):
+        k = int(rng.integers(3, 9))
+        q = S.query_random_walk(G, k, rng, tree=bool(i % 3 == 0), bias=1.0 if i % 2 else 0.0)
+        if q is None:
+            continue
+        p = O.plan(q.to_g_text(), enumerate_aut=0)
+        try:
+            O.match(og, p, limit=3_000_000)
+        except O.OracleError:
+            continue
+        check_case(ctx, g, og, q.to_g_text(), table=True, max_rows=1 << 22)
+        done += 1
+    assert done >= 15
+
+
+def test_level_overflow_deferral_gives_identical_results():
+    """A tiny SOLN_PREALLOC forces level buffers to fill; chunks are deferred
+    and re-run after the deeper levels drain.  Results must not change."""
+    G = S.rmat(12, 30000, seed=21, n_elabels=2)
+    src, dst, lab = G.directed()
+    og = O.Graph.from_edges(G.V, 3, src, dst, lab)
+    small = fm.Context(prealloc_bytes=256 << 20, soln_prealloc_bytes=24 << 20, output_prealloc_bytes=64 << 20,
+                       bank_rows=32)
+    g = fm.Graph.from_edges(small, G.V, 3, src, dst, lab)
+    q = S.query_path(5, [1, 2, 1, 2])
+    p = O.plan(q.to_g_text(), enumerate_aut=0)
+    oc = O.match(og, p)[0]
+    r = fm.match(small, g, fm.Query.from_text(q.to_g_text()), mode=fm.MODE_COUNT)
+    assert r.count == oc
+    assert r.launches > p.q - 1          # deferral happened
+    small.close()
+
+
+def test_table_truncation_keeps_exact_count():
+    V, s, d, l = complete_graph(30)
+    c = fm.Context(prealloc_bytes=128 << 20, soln_prealloc_bytes=32 << 20, output_prealloc_bytes=1 << 20,
+                   bank_rows=32)
+    g = fm.Graph.from_edges(c, V, 2, s, d, l)
+    q = fm.Query.from_text(S.query_cycle(4, [1] * 4).to_g_text())
+    r = fm.match(c, g, q, mode=fm.MODE_TABLE, allow_truncation=True)
+    assert r.count == math.perm(30, 4)
+    assert r.truncated and r.rows == (1 << 20) // 16
+    with pytest.raises(fm.FMError) as ei:
+        fm.match(c, g, q, mode=fm.MODE_TABLE)
+    assert ei.value.status == fm.FM_ERR_OUTPUT_OVERFLOW
+    c.close()
+
+
+def test_root_ranges_partition_the_count(ctx):
+    """Root-range partitioning (the multi-GPU split) sums to the full count."""
+    G = S.erdos_renyi(2000, 12000, seed=31, n_elabels=3)
+    src, dst, lab = G.directed()
+    g = fm.Graph.from_edges(ctx, G.V, 4, src, dst, lab)
+    q = fm.Query.from_text(S.query_cycle(4, [1, 2, 1, 2]).to_g_text())
+    full = fm.match(ctx, g, q, mode=fm.MODE_COUNT).count
+    cuts = [0, 333, 1000, 1001, 2000]
+    parts = [fm.match(ctx, g, q, mode=fm.MODE_COUNT, roots=(a, b)).count for a, b in zip(cuts, cuts[1:])]
+    assert sum(parts) == full and full > 0
+
+
+def test_query_id_columns(ctx):
+    G = S.erdos_renyi(300, 1500, seed=2, n_elabels=2)
+    src, dst, lab = G.directed()
+    g = fm.Graph.from_edges(ctx, G.V, 3, src, dst, lab)
+    qq = S.query_path(4, [1, 2, 1])
+    q = fm.Query.from_text(qq.to_g_text())
+    qi = q.info()
+    c1, ref_rows, _ = fm.match_table(ctx, g, q, columns=fm.COLUMNS_REFERENCE)
+    c2, id_rows, _ = fm.match_table(ctx, g, q, columns=fm.COLUMNS_QUERY_ID)
+    assert c1 == c2 > 0
+    # reference column i holds the vertex matched at depth q-1-i
+    order = [qi.order[d] for d in range(qi.q)]
+    perm = [order[qi.q - 1 - i] for i in range(qi.q)]      # original id of each reference column
+    conv = np.empty_like(ref_rows)
+    conv[:, perm] = ref_rows
+    assert np.array_equal(sorted_rows(conv), sorted_rows(id_rows))
+    assert all(len(set(r)) == qi.q for r in id_rows.tolist()[:1000])
+
+
+def test_single_vertex_and_single_edge_queries(ctx):
+    V, s, d, l = cycle_graph(50)
+    g = fm.Graph.from_edges(ctx, V, 2, s, d, l)
+    one = b"t # 0\n1 0 1 1\nv 0 1\nt # -1"
+    r = fm.match(ctx, g, fm.Query.from_text(one), mode=fm.MODE_COUNT)
+    assert r.count == 50
+    cnt, rows, _ = fm.match_table(ctx, g, fm.Query.from_text(one))
+    assert cnt == 50 and sorted(rows[:, 0].tolist()) == list(range(50))
+    r = fm.match(ctx, g, fm.Query.from_text(S.query_path(2, [1]).to_g_text()))
+    assert r.count == 100
+
+
+def test_text_and_edge_array_paths_agree(ctx):
+    G = S.erdos_renyi(1000, 2000, seed=1, n_elabels=87)
+    text = G.to_g_text()
+    g1 = fm.Graph.from_text(ctx, text)
+    src, dst, lab = G.directed()
+    g2 = fm.Graph.from_edges(ctx, G.V, 88, src, dst, lab)
+    i1, i2 = g1.info(), g2.info()
+    assert (i1.edges, i1.segments, i1.max_list, i1.nbr_words) == (i2.edges, i2.segments, i2.max_list, i2.nbr_words)
+
+
+@pytest.mark.parametrize("text,status", [
+    (b"t # 1\n2 0 1 1\nt # -1", 3),
+    (b"t # 0\n2 0 1 1\nt # -2", 4),
+    (b"t # 0\n2 x 1 1\nt # -1", 5),
+    (b"t # 0\n2 2 1 1\nv 0 1\nv 1 1\ne 0 1 1\nx 1 0 1\nt # -1", 6),
+    (b"t # 0\n2 2 1 1\nv 0 1\nv 1 1\ne 0 5 1\ne 1 0 1\nt # -1", 6),
+])
+def test_data_parser_errors(ctx, text, status):
+    with pytest.raises(fm.FMError) as ei:
+        fm.Graph.from_text(ctx, text)
+    assert ei.value.status == status
