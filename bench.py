@@ -190,7 +190,7 @@ def run_ours(args, rank, world, local):
     wl, G, (src, dst, lab), same, gen_s = load_workload(args.workload)
     queries_meta = wl["queries"]
     max_count = max(q["count"] for q in queries_meta)
-    out_bytes = int(max_count * 8 * 4 * 1.05) + (64 << 20)
+    out_bytes = ((int(max_count * 8 * 4 * 1.05) + (64 << 20)) >> 20) << 20
     ctx = fm.Context(prealloc_bytes=24 * GB + out_bytes + (64 << 20), soln_prealloc_bytes=24 * GB,
                      output_prealloc_bytes=out_bytes, bank_rows=1 << 16, device=local)
     t = time.time()

@@ -151,7 +151,9 @@ fm_status fm_context_create(const fm_knobs* knobs, fm_context** out) {
     if (knobs) k = *knobs;
     else fm_knobs_default(&k);
     if (k.bank_rows == 0) k.bank_rows = 1;
-    uint64_t need = k.soln_prealloc_bytes + k.output_prealloc_bytes + kMiscBytes;
+    // levels at [0, soln), table at round_up(soln, 256), control blocks at
+    // round_down(prealloc - misc, 256): the margin keeps the three disjoint
+    uint64_t need = ((k.soln_prealloc_bytes + 255) & ~255ull) + k.output_prealloc_bytes + kMiscBytes + 256;
     if (k.prealloc_bytes < need) {
         set_error("PREALLOC must cover SOLN_PREALLOC + OUTPUT_PREALLOC + 8 MiB");
         return FM_ERR_ARG;
@@ -172,7 +174,8 @@ fm_status fm_context_create(const fm_knobs* knobs, fm_context** out) {
     c->output_bytes = k.output_prealloc_bytes;
     c->soln = c->slab;
     c->output = (uint32_t*)(c->slab + ((k.soln_prealloc_bytes + 255) & ~255ull));
-    char* misc = c->slab + k.prealloc_bytes - kMiscBytes;
+    // control blocks hold 64-bit atomics: keep them 256-byte aligned whatever PREALLOC is
+    char* misc = c->slab + ((k.prealloc_bytes - kMiscBytes) & ~255ull);
     c->ctl = (LaunchCtl*)misc;
     c->tot = (MatchTotals*)(misc + 256);
     c->defs = (uint32_t*)(misc + 4096);

@@ -44,10 +44,17 @@ def check_case(ctx, g, og, qtext, expect_count=None, table=True, max_rows=1 << 2
     q = fm.Query.from_text(qtext)
     r = fm.match(ctx, g, q, mode=fm.MODE_COUNT)
     assert r.count == oc
-    for d in range(1, p.q):
+    # depth 1: every root is expanded (the lookup itself is the reference's
+    # root filter, src/smsm.cu:835), so the counters cover all V roots
+    if p.q > 1:
+        assert r.level[1].parents == og.V
+        assert r.level[1].lookups == og.V * p.nreq[1]
+    for d in range(2, p.q):
         assert r.level[d].lookups == ost.lookups[d], ("lookups", d)
         assert r.level[d].list_words == ost.list_words[d], ("list_words", d)
         assert r.level[d].parents == ost.partials[d - 1], ("parents", d)
+    for d in range(1, p.q - 1):
+        assert r.level[d].produced == ost.partials[d], ("produced", d)
     if table and oc <= max_rows:
         cnt, rows, r2 = fm.match_table(ctx, g, q, max_rows=max_rows)
         assert cnt == oc
