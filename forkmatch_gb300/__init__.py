@@ -19,6 +19,7 @@ FM_OK = 0
 FM_ERR_OUTPUT_OVERFLOW = 12
 MODE_TABLE, MODE_COUNT = 0, 1
 COLUMNS_REFERENCE, COLUMNS_QUERY_ID = 0, 1
+ORDER_AUTO, ORDER_REFERENCE = 0, 1
 
 STATUS_NAMES = {
     0: "FM_OK", 1: "FM_ERR_ARG", 2: "FM_ERR_IO", 3: "FM_ERR_DATA_HEADER0", 4: "FM_ERR_DATA_TRAILER",
@@ -62,7 +63,8 @@ class QueryInfo(ctypes.Structure):
 class MatchOpts(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("columns", ctypes.c_int32), ("stream", ctypes.c_void_p),
                 ("host_rows", ctypes.c_void_p), ("host_rows_cap", ctypes.c_uint64),
-                ("root_begin", ctypes.c_uint32), ("root_end", ctypes.c_uint32), ("profile", ctypes.c_int32)]
+                ("root_begin", ctypes.c_uint32), ("root_end", ctypes.c_uint32), ("profile", ctypes.c_int32),
+                ("order", ctypes.c_int32)]
 
 
 class LevelStats(ctypes.Structure):
@@ -264,7 +266,7 @@ class PinnedRows:
 
 
 def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_rows=None, roots=None,
-          profile=False, stream=None, allow_truncation=False):
+          profile=False, stream=None, allow_truncation=False, order=ORDER_AUTO):
     """Run fm_match.  Returns the Result struct; with ``host_rows`` (a
     PinnedRows or a C-contiguous uint32 numpy array) the table is copied there."""
     o = MatchOpts()
@@ -272,6 +274,7 @@ def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_ro
     o.mode = mode
     o.columns = columns
     o.profile = 1 if profile else 0
+    o.order = order
     if stream is not None:
         o.stream = stream
     if roots is not None:
@@ -289,9 +292,9 @@ def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_ro
     return r
 
 
-def match_table(ctx, graph, query, columns=COLUMNS_REFERENCE, max_rows=1 << 24):
+def match_table(ctx, graph, query, columns=COLUMNS_REFERENCE, max_rows=1 << 24, order=ORDER_AUTO):
     """Count and the table as a numpy array (rows copied to host)."""
     q = query.q
     buf = np.zeros(max_rows * q, dtype=np.uint32)
-    r = match(ctx, graph, query, mode=MODE_TABLE, columns=columns, host_rows=buf)
+    r = match(ctx, graph, query, mode=MODE_TABLE, columns=columns, host_rows=buf, order=order)
     return r.count, buf[: r.rows_copied * q].reshape(-1, q), r

@@ -229,6 +229,8 @@ static fm_status graph_from_host_arrays(fm_context* ctx, uint32_t V, uint32_t L,
         free_device_graph(g->g);
         return st;
     }
+    g->g.label_count.assign(L, 0);   // label frequencies for the matching-order cost model
+    for (uint64_t i = 0; i < E; i++) g->g.label_count[lab[i]]++;
     *out = g.release();
     return FM_OK;
 }
@@ -350,6 +352,7 @@ struct MatchRun {
     fm_context* ctx;
     const DeviceGraph* g;
     const Plan* plan;
+    const uint32_t* nreq_depth = nullptr;   // requirements per depth of the order in use
     ExpandParams base;
     cudaStream_t s;
     bool table;
@@ -369,7 +372,7 @@ struct MatchRun {
         uint32_t* def_b = def_a + ctx->def_cap;
         uint32_t ndef_in = 0;
         uint64_t fresh = 0;
-        const size_t smem = expand_smem_bytes(d, plan->nreq[d], block / 32);
+        const size_t smem = expand_smem_bytes(d, nreq_depth[d], block / 32);
         const int per_sm = expand_blocks_per_sm(mode, roots, dups, smem, block);
         while (true) {
             const uint64_t items = ndef_in + (n_chunks - fresh);
@@ -484,6 +487,27 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     const bool table = opts.mode == FM_MODE_TABLE;
     const uint64_t table_cap = ctx->output_bytes / (4ull * q);
 
+    // matching order: the reference's, or the cheapest one for this graph
+    uint32_t order[kMaxQ];
+    uint32_t nreq[kMaxQ], climb[kMaxQ][kMaxQ], rlab[kMaxQ][kMaxQ];
+    bool use_ref = opts.order == FM_ORDER_REFERENCE;
+    if (!use_ref) {
+        choose_order(pl, g, order);
+        if (!order_requirements(pl, order, nreq, climb, rlab)) use_ref = true;
+    }
+    if (use_ref) {
+        for (uint32_t d = 0; d < q; d++) {
+            order[d] = pl.order_local[d];
+            nreq[d] = pl.nreq[d];
+            for (uint32_t i = 0; i < pl.nreq[d]; i++) {
+                climb[d][i] = pl.req_climb[d][i];
+                rlab[d][i] = pl.req_label[d][i];
+            }
+        }
+    }
+    uint32_t ref_depth[kMaxQ];   // reference depth of each local vertex: fixes the table layout
+    for (uint32_t d = 0; d < q; d++) ref_depth[pl.order_local[d]] = d;
+
     // device plan
     MatchRun run;
     std::memset(&run.base, 0, sizeof(run.base));
@@ -492,15 +516,18 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     uint32_t r = 0;
     bool impossible = false;
     for (uint32_t d = 0; d < q; d++) {
-        dp.nreq[d] = pl.nreq[d];
+        dp.nreq[d] = nreq[d];
         dp.req_begin[d] = r;
-        for (uint32_t i = 0; i < pl.nreq[d]; i++, r++) {
-            dp.req_anc[r] = (uint8_t)(d - pl.req_climb[d][i]);
-            dp.req_label[r] = (uint8_t)pl.req_label[d][i];
-            if (pl.req_label[d][i] >= g.L) impossible = true;   // label absent from the data graph
+        for (uint32_t i = 0; i < nreq[d]; i++, r++) {
+            dp.req_anc[r] = (uint8_t)(d - climb[d][i]);
+            dp.req_label[r] = (uint8_t)rlab[d][i];
+            if (rlab[d][i] >= g.L) impossible = true;   // label absent from the data graph
         }
-        dp.out_col[d] = (uint8_t)(opts.columns == FM_COLUMNS_QUERY_ID ? pl.inv[pl.order_local[d]] : q - 1 - d);
+        const uint32_t v = order[d];
+        dp.out_col[d] = (uint8_t)(opts.columns == FM_COLUMNS_QUERY_ID ? pl.inv[v] : q - 1 - ref_depth[v]);
+        dp.col_depth[dp.out_col[d]] = (uint8_t)d;
     }
+    run.nreq_depth = nreq;
     if ((uint64_t)g.max_len * 32 >= (1ull << 32)) {
         set_error("a neighbour list is longer than 2^27");
         return FM_ERR_UNSUPPORTED;

@@ -42,21 +42,28 @@ struct DeviceGraph {
     int has_dups = 0;
     int device = 0;
     double build_ms = 0;
+    std::vector<uint64_t> label_count;   // e-lines per label slot
 };
 
 // ----------------------------------------------------------------- query plan
+struct LocalELine {
+    uint32_t a, b, l;                    // local a -> local b with label l
+};
+
 struct Plan {
     uint32_t q = 0;
     uint32_t e_lines = 0;
     uint32_t max_valency = 0;
     uint32_t inv[kMaxQ] = {};            // local -> original id
-    uint32_t order_local[kMaxQ] = {};    // depth -> local index
+    uint32_t order_local[kMaxQ] = {};    // reference matching order: depth -> local index
     uint32_t nreq[kMaxQ] = {};
     uint32_t req_climb[kMaxQ][kMaxQ] = {};
     uint32_t req_label[kMaxQ][kMaxQ] = {};
     uint32_t req_refl[kMaxQ][kMaxQ] = {};
     uint32_t pk_dist[kMaxQ] = {};
     uint64_t automorphisms = 0;
+    // e-lines of every local row, each row ordered by neighbour (the CCSR rows)
+    std::vector<LocalELine> rows;
 };
 
 // Device-side copy of a plan, passed by value to every expansion launch.
@@ -67,7 +74,16 @@ struct DevPlan {
     uint8_t req_anc[kMaxReqTotal];     // ancestor depth (row column) of each requirement
     uint8_t req_label[kMaxReqTotal];
     uint8_t out_col[kMaxQ];            // table column of the vertex matched at depth d
+    uint8_t col_depth[kMaxQ];          // depth whose vertex fills table column c
 };
+
+// Requirements of an arbitrary matching order (the reference's rule applied to
+// `order`): at depth d, the e-lines of the new vertex's row to vertices matched
+// earlier, ordered by climb.  Returns false if some depth >= 1 has none.
+bool order_requirements(const Plan& P, const uint32_t* order, uint32_t nreq[kMaxQ],
+                        uint32_t climb[kMaxQ][kMaxQ], uint32_t label[kMaxQ][kMaxQ]);
+// Cost-based matching order for a data graph (fm_parse.cpp).
+void choose_order(const Plan& P, const DeviceGraph& g, uint32_t order[kMaxQ]);
 
 // Per-launch control block in device memory.
 struct LaunchCtl {

@@ -13,11 +13,14 @@
 //      records -- k independent 16-byte loads, issued back to back;
 //   2. the shortest list is the driver; a warp prefix sum over driver lengths
 //      turns the 32 parents' candidate lists into one range of slots;
-//   3. lanes take 32 consecutive slots per round (load-balanced across
-//      parents, so a hub parent keeps all 32 lanes busy), test membership of
-//      the driver value in the other k-1 lists (inline compare or binary
-//      search), reject values already in the row, and append survivors with
-//      one atomic per warp round (__ballot_sync + __popc rank).
+//   3. lanes take 64 consecutive slots per round, two per lane with both
+//      driver loads in flight (load-balanced across parents, so a hub parent
+//      keeps all 32 lanes busy), reject values already in the row, test
+//      membership in the other k-1 lists (inline compare or binary search),
+//      and stage survivors in shared memory (__ballot_sync + __popc rank);
+//   4. a full stage (or the end of the chunk) is flushed with one atomic and
+//      fully coalesced stores: column by column into the next level, or as
+//      contiguous row-major rows into the table.
 // Lists of length <= 3 are inline in the segment record, so the common case
 // needs no second memory access.  With duplicate e-lines the value at rank r of
 // its run in the driver list survives only if every other list holds at least
@@ -83,20 +86,90 @@ __device__ __forceinline__ void defer_chunk(const ExpandParams& P, uint32_t chun
     else atomicOr(&P.ctl->error, 1u);
 }
 
+constexpr uint32_t kStage = 256;   // survivors staged per warp before one coalesced flush
+
+// Slot s of the warp's chunk belongs to parent j (the last j with excl[j] <= s),
+// at position t of that parent's driver list.
+__device__ __forceinline__ void slot_locate(uint32_t s, const uint32_t* excl_s, uint32_t& j, uint32_t& t) {
+    j = 0;
+#pragma unroll
+    for (uint32_t step = 16; step; step >>= 1)
+        if (excl_s[j + step] <= s) j += step;
+    t = s - excl_s[j];
+}
+
+// Does driver value x (position t of parent j's driver list dj) survive?
+// Injectivity first (shared memory only), then membership in the other lists.
+template <bool DUPS>
+__device__ __forceinline__ bool slot_check(const ExpandParams& P, uint32_t x, uint32_t t, uint32_t j, uint32_t dj,
+                                           const uint4& ds, const uint4* segs_s, const uint32_t* rows_s,
+                                           uint32_t k, uint32_t d) {
+    bool ok = true;
+    for (uint32_t c = 0; c < d && ok; c++) ok = rows_s[c * 32 + j] != x;
+    if (!ok) return false;
+    uint32_t need = 1;
+    if (DUPS) need = seg_rank(ds, t, x, P.nbr) + 1;
+    for (uint32_t i = 0; i < k && ok; i++) {
+        if (i == dj) continue;
+        ok = seg_has(segs_s[i * 32 + j], x, need, P.nbr);
+    }
+    return ok;
+}
+
+// Write the warp's staged survivors with one atomic: column by column into the
+// next level (SoA), or row-major into the table, every store coalesced.
+template <int MODE>
+__device__ __forceinline__ void flush_stage(const ExpandParams& P, uint32_t nst, uint32_t lane, uint32_t d,
+                                            const uint32_t* rows_s, const uint8_t* stj, const uint32_t* stx,
+                                            const uint8_t* col_depth_s) {
+    unsigned long long pos0 = 0;
+    if (lane == 0)
+        pos0 = atomicAdd(MODE == kModeMid ? &P.ctl->produced : &P.tot->table_pos, (unsigned long long)nst);
+    pos0 = __shfl_sync(kFull, pos0, 0);
+    if (MODE == kModeMid) {
+        for (uint32_t c = 0; c < d; c++) {
+            uint32_t* col = P.pout + c * P.ocap + pos0;
+            for (uint32_t i = lane; i < nst; i += 32) col[i] = rows_s[c * 32 + stj[i]];
+        }
+        uint32_t* col = P.pout + d * P.ocap + pos0;
+        for (uint32_t i = lane; i < nst; i += 32) col[i] = stx[i];
+    } else {
+        const uint32_t q = P.plan.q;
+        if (pos0 >= P.table_cap) return;
+        const uint64_t room = P.table_cap - pos0;
+        const uint32_t rows = nst < room ? nst : (uint32_t)room;
+        uint32_t* out = P.table + pos0 * q;
+        const uint32_t n = rows * q;
+        // row = w / q in single precision: w < 2^14 and the fractional part of
+        // (w + 0.5) / q stays >= 1/64 away from an integer, so it is exact
+        const float inv_q = 1.0f / (float)q;
+        for (uint32_t w = lane; w < n; w += 32) {
+            const uint32_t r = (uint32_t)(((float)w + 0.5f) * inv_q);
+            const uint32_t dep = col_depth_s[w - r * q];
+            out[w] = dep < d ? rows_s[dep * 32 + stj[r]] : stx[r];
+        }
+    }
+}
+
 template <int MODE, bool ROOTS, bool DUPS>
-__global__ void __launch_bounds__(kWarps * 32) k_expand(const __grid_constant__ ExpandParams P) {
+__global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant__ ExpandParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint8_t col_depth_s[kMaxQ];
+    if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P.plan.col_depth[threadIdx.x];
+    __syncthreads();
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = threadIdx.x >> 5;
     const uint32_t d = P.depth;
     const uint32_t k = P.plan.nreq[d];
     const uint32_t rb = P.plan.req_begin[d];
-    const uint32_t per_warp = 128 * d + 512 * k + 256;
+    const uint32_t per_warp = 128 * d + 512 * k + 256 + kStage * 5;
     unsigned char* ws = smem_raw + warp * per_warp;
-    uint32_t* rows_s = (uint32_t*)ws;                    // [d][32]
-    uint4* segs_s = (uint4*)(ws + 128 * d);              // [k][32]
-    uint32_t* excl_s = (uint32_t*)(ws + 128 * d + 512 * k);
-    uint32_t* drv_s = excl_s + 32;
+    uint32_t* rows_s = (uint32_t*)ws;                              // [d][32]
+    uint4* segs_s = (uint4*)(ws + 128 * d);                        // [k][32]
+    uint32_t* excl_s = (uint32_t*)(ws + 128 * d + 512 * k);        // [32]
+    uint32_t* drv_s = excl_s + 32;                                 // [32]
+    uint32_t* stx = (uint32_t*)(ws + 128 * d + 512 * k + 256);     // [kStage]
+    uint8_t* stj = (uint8_t*)(stx + kStage);                       // [kStage]
 
     unsigned long long n_count = 0, n_lookups = 0, n_words = 0, n_parents = 0;
 
@@ -165,49 +238,56 @@ __global__ void __launch_bounds__(kWarps * 32) k_expand(const __grid_constant__ 
         excl_s[lane] = incl - n;
         drv_s[lane] = drv;
         __syncwarp();
-        for (uint32_t base = 0; base < total; base += 32) {
-            const uint32_t s = base + lane;
-            bool ok = false;
-            uint32_t x = 0, j = 0;
-            if (s < total) {
-#pragma unroll
-                for (uint32_t step = 16; step; step >>= 1)
-                    if (excl_s[j + step] <= s) j += step;
-                const uint32_t t = s - excl_s[j];
-                const uint32_t dj = drv_s[j];
-                const uint4 ds = segs_s[dj * 32 + j];
-                x = seg_at(ds, t, P.nbr);
-                uint32_t need = 1;
-                if (DUPS) need = seg_rank(ds, t, x, P.nbr) + 1;
-                ok = true;
-                for (uint32_t i = 0; i < k && ok; i++) {
-                    if (i == dj) continue;
-                    ok = seg_has(segs_s[i * 32 + j], x, need, P.nbr);
-                }
-                for (uint32_t c = 0; c < d && ok; c++) ok = rows_s[c * 32 + j] != x;
+        uint32_t nst = 0;   // staged survivors (warp-uniform)
+        for (uint32_t base = 0; base < total; base += 64) {
+            const uint32_t s0 = base + lane, s1 = base + 32 + lane;
+            const bool a0 = s0 < total, a1 = s1 < total;
+            uint32_t j0 = 0, t0 = 0, j1 = 0, t1 = 0, x0 = 0, x1 = 0, dj0 = 0, dj1 = 0;
+            uint4 ds0 = make_uint4(0, 0, 0, 0), ds1 = make_uint4(0, 0, 0, 0);
+            // both driver loads are issued before either is used
+            if (a0) {
+                slot_locate(s0, excl_s, j0, t0);
+                dj0 = drv_s[j0];
+                ds0 = segs_s[dj0 * 32 + j0];
+                x0 = seg_at(ds0, t0, P.nbr);
             }
-            const unsigned ball = __ballot_sync(kFull, ok);
-            const uint32_t cnt = __popc(ball);
+            if (a1) {
+                slot_locate(s1, excl_s, j1, t1);
+                dj1 = drv_s[j1];
+                ds1 = segs_s[dj1 * 32 + j1];
+                x1 = seg_at(ds1, t1, P.nbr);
+            }
+            const bool ok0 = a0 && slot_check<DUPS>(P, x0, t0, j0, dj0, ds0, segs_s, rows_s, k, d);
+            const bool ok1 = a1 && slot_check<DUPS>(P, x1, t1, j1, dj1, ds1, segs_s, rows_s, k, d);
+            const unsigned b0 = __ballot_sync(kFull, ok0);
+            const unsigned b1 = __ballot_sync(kFull, ok1);
             if (MODE == kModeLastCount) {
-                n_count += cnt;
-            } else if (cnt) {
-                unsigned long long pos0 = 0;
-                if (lane == 0)
-                    pos0 = atomicAdd(MODE == kModeMid ? &P.ctl->produced : &P.tot->table_pos,
-                                     (unsigned long long)cnt);
-                pos0 = __shfl_sync(kFull, pos0, 0);
-                if (ok) {
-                    const uint64_t pos = pos0 + __popc(ball & ((1u << lane) - 1u));
-                    if (MODE == kModeMid) {
-                        for (uint32_t c = 0; c < d; c++) P.pout[c * P.ocap + pos] = rows_s[c * 32 + j];
-                        P.pout[d * P.ocap + pos] = x;
-                    } else if (pos < P.table_cap) {
-                        uint32_t* r = P.table + pos * P.plan.q;
-                        for (uint32_t c = 0; c < d; c++) r[P.plan.out_col[c]] = rows_s[c * 32 + j];
-                        r[P.plan.out_col[d]] = x;
-                    }
-                }
+                n_count += __popc(b0) + __popc(b1);
+                continue;
             }
+            const unsigned lt = (1u << lane) - 1u;
+            if (ok0) {
+                const uint32_t q0 = nst + __popc(b0 & lt);
+                stj[q0] = (uint8_t)j0;
+                stx[q0] = x0;
+            }
+            nst += __popc(b0);
+            if (ok1) {
+                const uint32_t q1 = nst + __popc(b1 & lt);
+                stj[q1] = (uint8_t)j1;
+                stx[q1] = x1;
+            }
+            nst += __popc(b1);
+            if (nst > kStage - 64) {
+                __syncwarp();
+                flush_stage<MODE>(P, nst, lane, d, rows_s, stj, stx, col_depth_s);
+                nst = 0;
+                __syncwarp();
+            }
+        }
+        if (MODE != kModeLastCount && nst) {
+            __syncwarp();
+            flush_stage<MODE>(P, nst, lane, d, rows_s, stj, stx, col_depth_s);
         }
         __syncwarp();
     }
@@ -249,7 +329,7 @@ void* pick(int mode, bool roots, bool dups) {
 }  // namespace
 
 size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps) {
-    return (size_t)warps * (128u * depth + 512u * nreq + 256u);
+    return (size_t)warps * (128u * depth + 512u * nreq + 256u + kStage * 5u);
 }
 
 int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block) {

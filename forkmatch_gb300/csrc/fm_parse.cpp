@@ -327,9 +327,11 @@ fm_status compile_query_text(const char* text, uint64_t len, Plan& P) {
     // Rows: (neighbour local, label) in e-line order, stable-sorted by neighbour.
     std::vector<std::vector<std::pair<uint32_t, uint32_t>>> row(q);
     for (const auto& e : es) row[loc[e.a]].push_back({loc[e.b], e.l});
-    for (auto& r : row) {
+    for (uint32_t v = 0; v < q; v++) {
+        auto& r = row[v];
         std::stable_sort(r.begin(), r.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
         P.max_valency = std::max<uint32_t>(P.max_valency, (uint32_t)r.size());
+        for (const auto& [m, l] : r) P.rows.push_back({v, m, l});
     }
     // Matching order: greedy, lowest local index on the frontier.
     int state[kMaxQ];
@@ -390,6 +392,107 @@ fm_status compile_query_text(const char* text, uint64_t len, Plan& P) {
     for (const auto& e : es) les.push_back({loc[e.a], loc[e.b], e.l});
     P.automorphisms = count_automorphisms(q, les);
     return FM_OK;
+}
+
+bool order_requirements(const Plan& P, const uint32_t* order, uint32_t nreq[kMaxQ],
+                        uint32_t climb[kMaxQ][kMaxQ], uint32_t label[kMaxQ][kMaxQ]) {
+    int depth_of[kMaxQ];
+    for (uint32_t i = 0; i < P.q; i++) depth_of[i] = -1;
+    for (uint32_t d = 0; d < P.q; d++) depth_of[order[d]] = (int)d;
+    for (uint32_t d = 0; d < P.q; d++) {
+        const uint32_t v = order[d];
+        uint32_t n = 0;
+        uint32_t c[kMaxQ], l[kMaxQ];
+        for (const auto& e : P.rows) {       // rows are grouped by a, ordered by neighbour
+            if (e.a != v || depth_of[e.b] < 0 || depth_of[e.b] >= (int)d) continue;
+            if (n == (uint32_t)kMaxQ) return false;
+            c[n] = d - (uint32_t)depth_of[e.b];
+            l[n] = e.l;
+            n++;
+        }
+        // stable sort by climb
+        for (uint32_t i = 1; i < n; i++) {
+            uint32_t cc = c[i], ll = l[i], j = i;
+            while (j > 0 && c[j - 1] > cc) { c[j] = c[j - 1]; l[j] = l[j - 1]; j--; }
+            c[j] = cc;
+            l[j] = ll;
+        }
+        if (d > 0 && n == 0) return false;
+        nreq[d] = n;
+        for (uint32_t i = 0; i < n; i++) { climb[d][i] = c[i]; label[d][i] = l[i]; }
+    }
+    return true;
+}
+
+// Greedy order by estimated growth, over every start vertex.  Under a random
+// graph model with the data graph's label frequencies, extending a partial
+// match by a vertex with back e-lines of labels l1..lk yields about
+//   min_i(E_li / V) * prod_{other i}(E_li / V^2)
+// candidates: the shortest list drives, each further list filters.  Each step
+// takes the vertex with the smallest factor (so cycles close as early as
+// possible), ties broken by more back e-lines, larger degree, lower local
+// index; the start with the smallest summed partial-match estimate wins, and
+// ties keep the reference's start (local index 0 comes first).
+void choose_order(const Plan& P, const DeviceGraph& g, uint32_t order[kMaxQ]) {
+    const uint32_t q = P.q;
+    for (uint32_t d = 0; d < q; d++) order[d] = P.order_local[d];
+    if (q <= 2 || g.V == 0) return;
+    const double V = (double)g.V;
+    auto avg = [&](uint32_t l) {
+        uint64_t c = l < g.label_count.size() ? g.label_count[l] : 0;
+        return (double)c / V;
+    };
+    uint32_t deg[kMaxQ] = {};
+    for (const auto& e : P.rows) deg[e.a]++;
+    double best = -1;
+    uint32_t cand[kMaxQ];
+    for (uint32_t start = 0; start < q; start++) {
+        bool matched[kMaxQ] = {};
+        matched[start] = true;
+        cand[0] = start;
+        double card = V, cost = V;
+        bool ok = true;
+        for (uint32_t d = 1; d < q && ok; d++) {
+            int pick = -1;
+            double pf = 0;
+            uint32_t pback = 0;
+            for (uint32_t v = 0; v < q; v++) {
+                if (matched[v]) continue;
+                double mn = 1e300, prod = 1.0;
+                uint32_t back = 0;
+                for (const auto& e : P.rows) {
+                    if (e.a != v || !matched[e.b]) continue;
+                    double a = avg(e.l);
+                    back++;
+                    if (a < mn) {
+                        if (mn < 1e299) prod *= mn / V;
+                        mn = a;
+                    } else {
+                        prod *= a / V;
+                    }
+                }
+                if (!back) continue;
+                double f = mn * prod;
+                bool better = pick < 0 || f < pf * (1 - 1e-12) ||
+                              (f <= pf * (1 + 1e-12) && (back > pback || (back == pback && deg[v] > deg[pick])));
+                if (better) {
+                    pick = (int)v;
+                    pf = f;
+                    pback = back;
+                }
+            }
+            if (pick < 0) { ok = false; break; }
+            matched[pick] = true;
+            cand[d] = (uint32_t)pick;
+            card *= pf;
+            cost += card;
+        }
+        if (!ok) continue;
+        if (best < 0 || cost < best * (1 - 1e-9)) {
+            best = cost;
+            for (uint32_t d = 0; d < q; d++) order[d] = cand[d];
+        }
+    }
 }
 
 }  // namespace fm

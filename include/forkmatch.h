@@ -158,7 +158,17 @@ typedef struct fm_match_opts {
     uint32_t root_begin;        /* roots (depth-0 images) in [root_begin, root_end); */
     uint32_t root_end;          /*   root_end == 0 means all vertices */
     int32_t profile;            /* 1: time every expansion launch with CUDA events */
+    int32_t order;              /* fm_order: matching order used internally */
 } fm_match_opts;
+
+/* Matching order.  Results (count, row set, column layout) do not depend on
+ * it; only the work does.  FM_ORDER_AUTO picks the order with the smallest
+ * estimated partial-match volume for the data graph (cycles closed early);
+ * FM_ORDER_REFERENCE uses the reference's greedy order (src/ccsr.cuh:229-326). */
+typedef enum fm_order {
+    FM_ORDER_AUTO = 0,
+    FM_ORDER_REFERENCE = 1
+} fm_order;
 
 void fm_match_opts_default(fm_match_opts* o);
 

@@ -42,10 +42,17 @@ def check_case(ctx, g, og, qtext, expect_count=None, table=True, max_rows=1 << 2
     if expect_count is not None:
         assert oc == expect_count
     q = fm.Query.from_text(qtext)
-    r = fm.match(ctx, g, q, mode=fm.MODE_COUNT)
+    # the cost-based order must not change the result
+    assert fm.match(ctx, g, q, mode=fm.MODE_COUNT, order=fm.ORDER_AUTO).count == oc
+    # with the reference order the per-level work equals the oracle's exactly
+    r = fm.match(ctx, g, q, mode=fm.MODE_COUNT, order=fm.ORDER_REFERENCE)
     assert r.count == oc
     # depth 1: every root is expanded (the lookup itself is the reference's
     # root filter, src/smsm.cu:835), so the counters cover all V roots
+    if r.launches == 0:
+        # a query label is absent from the graph: no launch is needed
+        assert oc == 0
+        return oc
     if p.q > 1:
         assert r.level[1].parents == og.V
         assert r.level[1].lookups == og.V * p.nreq[1]
@@ -56,9 +63,11 @@ def check_case(ctx, g, og, qtext, expect_count=None, table=True, max_rows=1 << 2
     for d in range(1, p.q - 1):
         assert r.level[d].produced == ost.partials[d], ("produced", d)
     if table and oc <= max_rows:
-        cnt, rows, r2 = fm.match_table(ctx, g, q, max_rows=max_rows)
-        assert cnt == oc
-        assert np.array_equal(sorted_rows(rows), sorted_rows(orows))
+        want = sorted_rows(orows)
+        for order in (fm.ORDER_AUTO, fm.ORDER_REFERENCE):
+            cnt, rows, r2 = fm.match_table(ctx, g, q, max_rows=max_rows, order=order)
+            assert cnt == oc
+            assert np.array_equal(sorted_rows(rows), want)
     return oc
 
 
