@@ -49,6 +49,8 @@ struct fm_context {
     MatchTotals* tot = nullptr; // device
     uint32_t* defs = nullptr;   // 2 deferred lists per depth
     uint32_t def_cap = 0;
+    HeavyEntry* heavy = nullptr;  // heavy-chunk entries of the current launch
+    uint32_t heavy_cap = 0;
     LaunchCtl* h_ctl = nullptr; // pinned mirrors
     MatchTotals* h_tot = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -65,7 +67,7 @@ uint64_t env_u64(const char* name, uint64_t dflt) {
     return (end && *end == 0) ? (uint64_t)x : dflt;
 }
 
-constexpr uint64_t kMiscBytes = 8ull << 20;
+constexpr uint64_t kMiscBytes = 16ull << 20;
 
 }  // namespace
 
@@ -155,7 +157,7 @@ fm_status fm_context_create(const fm_knobs* knobs, fm_context** out) {
     // round_down(prealloc - misc, 256): the margin keeps the three disjoint
     uint64_t need = ((k.soln_prealloc_bytes + 255) & ~255ull) + k.output_prealloc_bytes + kMiscBytes + 256;
     if (k.prealloc_bytes < need) {
-        set_error("PREALLOC must cover SOLN_PREALLOC + OUTPUT_PREALLOC + 8 MiB");
+        set_error("PREALLOC must cover SOLN_PREALLOC + OUTPUT_PREALLOC + 16 MiB");
         return FM_ERR_ARG;
     }
     std::unique_ptr<fm_context, void (*)(fm_context*)> c(new fm_context(), fm_context_destroy);
@@ -176,10 +178,14 @@ fm_status fm_context_create(const fm_knobs* knobs, fm_context** out) {
     c->output = (uint32_t*)(c->slab + ((k.soln_prealloc_bytes + 255) & ~255ull));
     // control blocks hold 64-bit atomics: keep them 256-byte aligned whatever PREALLOC is
     char* misc = c->slab + ((k.prealloc_bytes - kMiscBytes) & ~255ull);
+    // [0, 4 KiB) control blocks, [4 KiB, 8 MiB) deferred-chunk lists,
+    // [8 MiB, 16 MiB) heavy-chunk entries
     c->ctl = (LaunchCtl*)misc;
-    c->tot = (MatchTotals*)(misc + 256);
+    c->tot = (MatchTotals*)(misc + 512);
     c->defs = (uint32_t*)(misc + 4096);
-    c->def_cap = (uint32_t)((kMiscBytes - 4096) / 4 / (2 * kMaxQ));
+    c->def_cap = (uint32_t)(((8ull << 20) - 4096) / 4 / (2 * kMaxQ));
+    c->heavy = (HeavyEntry*)(misc + (8ull << 20));
+    c->heavy_cap = (uint32_t)((kMiscBytes - (8ull << 20)) / sizeof(HeavyEntry));
     FM_CUDA(cudaHostAlloc(&c->h_ctl, sizeof(LaunchCtl), cudaHostAllocDefault));
     FM_CUDA(cudaHostAlloc(&c->h_tot, sizeof(MatchTotals), cudaHostAllocDefault));
     FM_CUDA(cudaEventCreate(&c->ev0));
@@ -490,7 +496,10 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     // matching order: the reference's, or the cheapest one for this graph
     uint32_t order[kMaxQ];
     uint32_t nreq[kMaxQ], climb[kMaxQ][kMaxQ], rlab[kMaxQ][kMaxQ];
-    bool use_ref = opts.order == FM_ORDER_REFERENCE;
+    // With duplicate e-lines the reference's multiplicity is a per-depth
+    // minimum over the intersected lists (src/smsm.cu:73-140), which depends on
+    // which back edges share a depth: only its own order reproduces its count.
+    bool use_ref = opts.order == FM_ORDER_REFERENCE || g.has_dups;
     if (!use_ref) {
         choose_order(pl, g, order);
         if (!order_requirements(pl, order, nreq, climb, rlab)) use_ref = true;
@@ -578,6 +587,8 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         b.table_cap = table_cap;
         b.ctl = ctx->ctl;
         b.tot = ctx->tot;
+        b.heavy = ctx->heavy;
+        b.heavy_cap = ctx->heavy_cap;
         fm_status st = run.launch_level(1, re - rb, true);
         if (st != FM_OK) return st;
     }

@@ -97,6 +97,17 @@ struct LaunchCtl {
     unsigned int ndef;              // deferred chunks written
     unsigned int error;
     unsigned int pad;
+    unsigned long long heavy;       // heavy chunks: (entries << 32) | pieces, one packed atomic
+    unsigned long long claim2;      // heavy pieces claimed
+};
+
+// A chunk whose candidate range is too long for one warp: its slots are cut
+// into pieces of kHeavyPiece and spread over every warp of a second launch.
+struct HeavyEntry {
+    uint32_t chunk;
+    uint32_t total;                 // candidate slots of the chunk
+    uint32_t piece0;                // first global piece index
+    uint32_t pieces;
 };
 
 // Per-match totals in device memory.
@@ -135,9 +146,13 @@ struct ExpandParams {
     uint64_t table_cap;
     LaunchCtl* ctl;
     MatchTotals* tot;
+    HeavyEntry* heavy;
+    uint32_t heavy_cap;             // entries; chunks are published only while room remains
+    uint32_t max_warps;             // warps of the launch (bounds concurrent publishers)
 };
 
-// Launch one expansion kernel (fm_match.cu).
+// Launch one level expansion: the main pass, then the heavy-chunk pass
+// (fm_match.cu).
 cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups, int grid, int block,
                           size_t smem, cudaStream_t s);
 size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps);

@@ -151,6 +151,138 @@ __device__ __forceinline__ void flush_stage(const ExpandParams& P, uint32_t nst,
     }
 }
 
+constexpr uint32_t kHeavyThresh = 2048;   // candidate slots above which a chunk is split
+constexpr uint32_t kHeavyPiece = 1024;    // slots per piece of a split chunk
+constexpr uint32_t kHeavyMaxPieces = 65536;
+
+// Per-warp shared memory for one chunk of 32 parents.
+struct WarpMem {
+    uint32_t* rows_s;   // [d][32] parent rows, column-major
+    uint4* segs_s;      // [k][32] segment records
+    uint32_t* excl_s;   // [32] exclusive prefix of driver lengths
+    uint32_t* drv_s;    // [32] driver list of each parent
+    uint32_t* stx;      // [kStage] staged survivor values
+    uint8_t* stj;       // [kStage] staged survivor parents
+};
+
+__device__ __forceinline__ WarpMem warp_mem(unsigned char* smem_raw, uint32_t warp, uint32_t d, uint32_t k) {
+    const uint32_t per_warp = 128 * d + 512 * k + 256 + kStage * 5;
+    unsigned char* ws = smem_raw + warp * per_warp;
+    WarpMem m;
+    m.rows_s = (uint32_t*)ws;
+    m.segs_s = (uint4*)(ws + 128 * d);
+    m.excl_s = (uint32_t*)(ws + 128 * d + 512 * k);
+    m.drv_s = m.excl_s + 32;
+    m.stx = (uint32_t*)(ws + 128 * d + 512 * k + 256);
+    m.stj = (uint8_t*)(m.stx + kStage);
+    return m;
+}
+
+// Load the 32 parents of `chunk`, look up their k lists (independent 16-byte
+// loads), pick each parent's shortest list as its driver and prefix-sum the
+// driver lengths.  Returns the chunk's candidate slots (warp-uniform).
+template <bool ROOTS>
+__device__ __forceinline__ uint32_t load_chunk(const ExpandParams& P, const WarpMem& m, uint32_t chunk, uint32_t lane,
+                                               uint32_t d, uint32_t k, uint32_t rb, bool& valid,
+                                               unsigned long long& words) {
+    const uint64_t p = (uint64_t)chunk * 32 + lane;
+    valid = p < P.n_parents;
+    if (ROOTS) {
+        m.rows_s[lane] = P.root_begin + (uint32_t)p;
+    } else {
+        for (uint32_t c = 0; c < d; c++) m.rows_s[c * 32 + lane] = valid ? P.pin[c * P.pstride + p] : 0u;
+    }
+    uint32_t n = 0, drv = 0;
+    words = 0;
+    if (valid) {
+        uint32_t best = 0xffffffffu;
+        for (uint32_t i = 0; i < k; i++) {
+            const uint32_t anc = P.plan.req_anc[rb + i];
+            const uint32_t lab = P.plan.req_label[rb + i];
+            const uint32_t v = m.rows_s[anc * 32 + lane];
+            const uint4 sg = ldg4(P.seg + (uint64_t)lab * P.V + v);
+            m.segs_s[i * 32 + lane] = sg;
+            words += sg.x;
+            if (sg.x < best) {
+                best = sg.x;
+                drv = i;
+            }
+        }
+        n = best;
+    }
+    uint32_t incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if ((int)lane >= o) incl += t;
+    }
+    m.excl_s[lane] = incl - n;
+    m.drv_s[lane] = drv;
+    __syncwarp();
+    return __shfl_sync(kFull, incl, 31);
+}
+
+// Evaluate slots [begin, end) of the loaded chunk: two slots per lane per round
+// with both driver loads in flight, survivors staged and flushed coalesced.
+template <int MODE, bool DUPS>
+__device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpMem& m, uint32_t begin, uint32_t end,
+                                              uint32_t lane, uint32_t d, uint32_t k, const uint8_t* col_depth_s,
+                                              unsigned long long& n_count) {
+    uint32_t nst = 0;   // staged survivors (warp-uniform)
+    for (uint32_t base = begin; base < end; base += 64) {
+        const uint32_t s0 = base + lane, s1 = base + 32 + lane;
+        const bool a0 = s0 < end, a1 = s1 < end;
+        uint32_t j0 = 0, t0 = 0, j1 = 0, t1 = 0, x0 = 0, x1 = 0, dj0 = 0, dj1 = 0;
+        uint4 ds0 = make_uint4(0, 0, 0, 0), ds1 = make_uint4(0, 0, 0, 0);
+        if (a0) {
+            slot_locate(s0, m.excl_s, j0, t0);
+            dj0 = m.drv_s[j0];
+            ds0 = m.segs_s[dj0 * 32 + j0];
+            x0 = seg_at(ds0, t0, P.nbr);
+        }
+        if (a1) {
+            slot_locate(s1, m.excl_s, j1, t1);
+            dj1 = m.drv_s[j1];
+            ds1 = m.segs_s[dj1 * 32 + j1];
+            x1 = seg_at(ds1, t1, P.nbr);
+        }
+        const bool ok0 = a0 && slot_check<DUPS>(P, x0, t0, j0, dj0, ds0, m.segs_s, m.rows_s, k, d);
+        const bool ok1 = a1 && slot_check<DUPS>(P, x1, t1, j1, dj1, ds1, m.segs_s, m.rows_s, k, d);
+        const unsigned b0 = __ballot_sync(kFull, ok0);
+        const unsigned b1 = __ballot_sync(kFull, ok1);
+        if (MODE == kModeLastCount) {
+            n_count += __popc(b0) + __popc(b1);
+            continue;
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        if (ok0) {
+            const uint32_t q0 = nst + __popc(b0 & lt);
+            m.stj[q0] = (uint8_t)j0;
+            m.stx[q0] = x0;
+        }
+        nst += __popc(b0);
+        if (ok1) {
+            const uint32_t q1 = nst + __popc(b1 & lt);
+            m.stj[q1] = (uint8_t)j1;
+            m.stx[q1] = x1;
+        }
+        nst += __popc(b1);
+        if (nst > kStage - 64) {
+            __syncwarp();
+            flush_stage<MODE>(P, nst, lane, d, m.rows_s, m.stj, m.stx, col_depth_s);
+            nst = 0;
+            __syncwarp();
+        }
+    }
+    if (MODE != kModeLastCount && nst) {
+        __syncwarp();
+        flush_stage<MODE>(P, nst, lane, d, m.rows_s, m.stj, m.stx, col_depth_s);
+    }
+    __syncwarp();
+}
+
+// Main pass: warps claim chunks of 32 parents; long candidate ranges are
+// published to the heavy list instead of being walked by one warp.
 template <int MODE, bool ROOTS, bool DUPS>
 __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant__ ExpandParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -158,21 +290,12 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
     if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P.plan.col_depth[threadIdx.x];
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t warp = threadIdx.x >> 5;
     const uint32_t d = P.depth;
     const uint32_t k = P.plan.nreq[d];
     const uint32_t rb = P.plan.req_begin[d];
-    const uint32_t per_warp = 128 * d + 512 * k + 256 + kStage * 5;
-    unsigned char* ws = smem_raw + warp * per_warp;
-    uint32_t* rows_s = (uint32_t*)ws;                              // [d][32]
-    uint4* segs_s = (uint4*)(ws + 128 * d);                        // [k][32]
-    uint32_t* excl_s = (uint32_t*)(ws + 128 * d + 512 * k);        // [32]
-    uint32_t* drv_s = excl_s + 32;                                 // [32]
-    uint32_t* stx = (uint32_t*)(ws + 128 * d + 512 * k + 256);     // [kStage]
-    uint8_t* stj = (uint8_t*)(stx + kStage);                       // [kStage]
+    const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k);
 
     unsigned long long n_count = 0, n_lookups = 0, n_words = 0, n_parents = 0;
-
     for (;;) {
         unsigned long long item = 0;
         if (lane == 0) item = atomicAdd(&P.ctl->claim, 1ull);
@@ -185,38 +308,9 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
                 break;
             }
         }
-        const uint64_t p = (uint64_t)chunk * 32 + lane;
-        const bool valid = p < P.n_parents;
-        if (ROOTS) {
-            rows_s[lane] = P.root_begin + (uint32_t)p;
-        } else {
-            for (uint32_t c = 0; c < d; c++) rows_s[c * 32 + lane] = valid ? P.pin[c * P.pstride + p] : 0u;
-        }
-        uint32_t n = 0, drv = 0;
-        unsigned long long w = 0;
-        if (valid) {
-            uint32_t best = 0xffffffffu;
-            for (uint32_t i = 0; i < k; i++) {
-                const uint32_t anc = P.plan.req_anc[rb + i];
-                const uint32_t lab = P.plan.req_label[rb + i];
-                const uint32_t v = rows_s[anc * 32 + lane];
-                const uint4 s = ldg4(P.seg + (uint64_t)lab * P.V + v);
-                segs_s[i * 32 + lane] = s;
-                w += s.x;
-                if (s.x < best) {
-                    best = s.x;
-                    drv = i;
-                }
-            }
-            n = best;
-        }
-        uint32_t incl = n;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t t = __shfl_up_sync(kFull, incl, o);
-            if ((int)lane >= o) incl += t;
-        }
-        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        bool valid;
+        unsigned long long w;
+        const uint32_t total = load_chunk<ROOTS>(P, m, chunk, lane, d, k, rb, valid, w);
         if (MODE == kModeMid) {
             int ok = 1;
             if (lane == 0 && total) {
@@ -235,63 +329,31 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
             n_words += w;
             n_parents += 1;
         }
-        excl_s[lane] = incl - n;
-        drv_s[lane] = drv;
-        __syncwarp();
-        uint32_t nst = 0;   // staged survivors (warp-uniform)
-        for (uint32_t base = 0; base < total; base += 64) {
-            const uint32_t s0 = base + lane, s1 = base + 32 + lane;
-            const bool a0 = s0 < total, a1 = s1 < total;
-            uint32_t j0 = 0, t0 = 0, j1 = 0, t1 = 0, x0 = 0, x1 = 0, dj0 = 0, dj1 = 0;
-            uint4 ds0 = make_uint4(0, 0, 0, 0), ds1 = make_uint4(0, 0, 0, 0);
-            // both driver loads are issued before either is used
-            if (a0) {
-                slot_locate(s0, excl_s, j0, t0);
-                dj0 = drv_s[j0];
-                ds0 = segs_s[dj0 * 32 + j0];
-                x0 = seg_at(ds0, t0, P.nbr);
+        if (total > kHeavyThresh) {
+            // Publish: one packed atomic reserves the entry index and its piece
+            // range, so entries are ordered by first piece.  The room check is
+            // conservative: at most max_warps publishers can be past it at once.
+            int pub = 0;
+            const uint32_t np = (total + kHeavyPiece - 1) / kHeavyPiece;
+            if (lane == 0 && np <= kHeavyMaxPieces) {
+                const unsigned long long h = *(volatile unsigned long long*)&P.ctl->heavy;
+                if ((uint32_t)(h >> 32) + P.max_warps < P.heavy_cap && (uint32_t)h < (1u << 31)) {
+                    const unsigned long long old = atomicAdd(&P.ctl->heavy, (1ull << 32) | np);
+                    HeavyEntry e;
+                    e.chunk = chunk;
+                    e.total = total;
+                    e.piece0 = (uint32_t)old;
+                    e.pieces = np;
+                    P.heavy[(uint32_t)(old >> 32)] = e;
+                    pub = 1;
+                }
             }
-            if (a1) {
-                slot_locate(s1, excl_s, j1, t1);
-                dj1 = drv_s[j1];
-                ds1 = segs_s[dj1 * 32 + j1];
-                x1 = seg_at(ds1, t1, P.nbr);
-            }
-            const bool ok0 = a0 && slot_check<DUPS>(P, x0, t0, j0, dj0, ds0, segs_s, rows_s, k, d);
-            const bool ok1 = a1 && slot_check<DUPS>(P, x1, t1, j1, dj1, ds1, segs_s, rows_s, k, d);
-            const unsigned b0 = __ballot_sync(kFull, ok0);
-            const unsigned b1 = __ballot_sync(kFull, ok1);
-            if (MODE == kModeLastCount) {
-                n_count += __popc(b0) + __popc(b1);
-                continue;
-            }
-            const unsigned lt = (1u << lane) - 1u;
-            if (ok0) {
-                const uint32_t q0 = nst + __popc(b0 & lt);
-                stj[q0] = (uint8_t)j0;
-                stx[q0] = x0;
-            }
-            nst += __popc(b0);
-            if (ok1) {
-                const uint32_t q1 = nst + __popc(b1 & lt);
-                stj[q1] = (uint8_t)j1;
-                stx[q1] = x1;
-            }
-            nst += __popc(b1);
-            if (nst > kStage - 64) {
-                __syncwarp();
-                flush_stage<MODE>(P, nst, lane, d, rows_s, stj, stx, col_depth_s);
-                nst = 0;
-                __syncwarp();
-            }
+            pub = __shfl_sync(kFull, pub, 0);
+            if (pub) continue;
         }
-        if (MODE != kModeLastCount && nst) {
-            __syncwarp();
-            flush_stage<MODE>(P, nst, lane, d, rows_s, stj, stx, col_depth_s);
-        }
-        __syncwarp();
+        process_slots<MODE, DUPS>(P, m, 0, total, lane, d, k, col_depth_s, n_count);
     }
-    // commit statistics: one atomic per warp per counter
+    // statistics: one atomic per warp per counter
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
         n_lookups += __shfl_down_sync(kFull, n_lookups, o);
@@ -308,16 +370,57 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
     }
 }
 
+// Heavy pass (same stream, after the main pass): every warp claims pieces of
+// the published chunks, reloads that chunk and walks its piece of the slots.
+// The main pass already reserved the chunk's output budget and counted its work.
 template <int MODE, bool ROOTS, bool DUPS>
-void* kernel_ptr() {
-    return (void*)&k_expand<MODE, ROOTS, DUPS>;
+__global__ void __launch_bounds__(kWarps * 32, 4) k_expand_heavy(const __grid_constant__ ExpandParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint8_t col_depth_s[kMaxQ];
+    if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P.plan.col_depth[threadIdx.x];
+    __syncthreads();
+    const unsigned long long h = P.ctl->heavy;
+    const uint32_t nent = (uint32_t)(h >> 32);
+    const uint32_t npieces = (uint32_t)h;
+    if (nent == 0) return;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t d = P.depth;
+    const uint32_t k = P.plan.nreq[d];
+    const uint32_t rb = P.plan.req_begin[d];
+    const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k);
+    unsigned long long n_count = 0;
+    for (;;) {
+        unsigned long long gp = 0;
+        if (lane == 0) gp = atomicAdd(&P.ctl->claim2, 1ull);
+        gp = __shfl_sync(kFull, gp, 0);
+        if (gp >= npieces) break;
+        uint32_t lo = 0, hi = nent;      // last entry with piece0 <= gp
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (P.heavy[mid].piece0 <= gp) lo = mid;
+            else hi = mid;
+        }
+        const HeavyEntry e = P.heavy[lo];
+        const uint32_t begin = ((uint32_t)gp - e.piece0) * kHeavyPiece;
+        const uint32_t end = min(begin + kHeavyPiece, e.total);
+        bool valid;
+        unsigned long long w;
+        load_chunk<ROOTS>(P, m, e.chunk, lane, d, k, rb, valid, w);
+        process_slots<MODE, DUPS>(P, m, begin, end, lane, d, k, col_depth_s, n_count);
+    }
+    if (MODE == kModeLastCount && lane == 0 && n_count) atomicAdd(&P.tot->count, n_count);
 }
 
-void* pick(int mode, bool roots, bool dups) {
-#define FM_PICK(M)                                                                         \
-    if (mode == M) {                                                                       \
-        if (roots) return dups ? kernel_ptr<M, true, true>() : kernel_ptr<M, true, false>(); \
-        return dups ? kernel_ptr<M, false, true>() : kernel_ptr<M, false, false>();        \
+template <int MODE, bool ROOTS, bool DUPS>
+void* kernel_ptr(bool heavy) {
+    return heavy ? (void*)&k_expand_heavy<MODE, ROOTS, DUPS> : (void*)&k_expand<MODE, ROOTS, DUPS>;
+}
+
+void* pick(int mode, bool roots, bool dups, bool heavy) {
+#define FM_PICK(M)                                                                                         \
+    if (mode == M) {                                                                                       \
+        if (roots) return dups ? kernel_ptr<M, true, true>(heavy) : kernel_ptr<M, true, false>(heavy);     \
+        return dups ? kernel_ptr<M, false, true>(heavy) : kernel_ptr<M, false, false>(heavy);              \
     }
     FM_PICK(kModeMid)
     FM_PICK(kModeLastTable)
@@ -333,8 +436,11 @@ size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps) {
 }
 
 int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block) {
-    void* f = pick(mode, roots, dups);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    void* f = pick(mode, roots, dups, false);
+    if (smem > 48 * 1024) {
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(pick(mode, roots, dups, true), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, block, smem) != cudaSuccess || n < 1) n = 1;
     return n;
@@ -342,10 +448,15 @@ int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block
 
 cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups, int grid, int block,
                           size_t smem, cudaStream_t s) {
-    void* f = pick(mode, roots, dups);
-    if (!f) return cudaErrorInvalidValue;
-    void* args[] = {(void*)&p};
-    return cudaLaunchKernel(f, dim3(grid), dim3(block), args, smem, s);
+    void* f = pick(mode, roots, dups, false);
+    void* fh = pick(mode, roots, dups, true);
+    if (!f || !fh) return cudaErrorInvalidValue;
+    ExpandParams q = p;
+    q.max_warps = (uint32_t)grid * (uint32_t)(block / 32);
+    void* args[] = {(void*)&q};
+    cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(block), args, smem, s);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchKernel(fh, dim3(grid), dim3(block), args, smem, s);
 }
 
 }  // namespace fm

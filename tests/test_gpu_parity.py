@@ -110,6 +110,32 @@ def test_star_and_cycle_closed_forms(ctx):
         assert r.count == 2000
 
 
+def test_heavy_chunks_split_across_warps(ctx):
+    """Hub lists longer than one warp's share (> 2048 candidate slots per
+    chunk) are cut into pieces for every warp; counts and rows must not change.
+    K_{2,n}: 4-cycles = 8 * C(n, 2), 2-stars centred anywhere = 2*n*(n-1) + n*2."""
+    n = 3000
+    hubs = np.array([0, 1], dtype=np.uint32)
+    leaves = np.arange(2, n + 2, dtype=np.uint32)
+    a = np.repeat(hubs, n)
+    b = np.tile(leaves, 2)
+    src = np.concatenate([a, b])
+    dst = np.concatenate([b, a])
+    lab = np.ones(len(src), dtype=np.uint32)
+    g = fm.Graph.from_edges(ctx, n + 2, 2, src, dst, lab)
+    og = O.Graph.from_edges(n + 2, 2, src, dst, lab)
+    c4 = S.query_cycle(4, [1] * 4).to_g_text()
+    want = 8 * math.comb(n, 2)
+    for order in (fm.ORDER_AUTO, fm.ORDER_REFERENCE):
+        assert fm.match(ctx, g, fm.Query.from_text(c4), mode=fm.MODE_COUNT, order=order).count == want
+    cnt, rows, _ = fm.match_table(ctx, g, fm.Query.from_text(c4), max_rows=want)
+    assert cnt == want
+    ocnt, orows, _ = O.match(og, O.plan(c4, enumerate_aut=0), table=True, table_cap=want)
+    assert np.array_equal(sorted_rows(rows), sorted_rows(orows))
+    p3 = S.query_path(3, [1, 1]).to_g_text()
+    assert fm.match(ctx, g, fm.Query.from_text(p3), mode=fm.MODE_COUNT).count == 2 * n * (n - 1) + n * 2
+
+
 def test_label_mismatch_and_absent_label(ctx):
     V, s, d, l = complete_graph(6, label=2)
     g = fm.Graph.from_edges(ctx, V, 3, s, d, l)
