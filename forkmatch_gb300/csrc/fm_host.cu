@@ -411,7 +411,7 @@ struct MatchRun {
                 e1 = ctx->prof[prof_used + 1];
                 FM_CUDA(cudaEventRecord(e0, s));
             }
-            FM_CUDA(launch_expand(p, mode, roots, dups, grid, block, smem, s));
+            FM_CUDA(launch_expand(p, mode, roots, dups, grid, ctx->sms * per_sm, block, smem, s));
             if (profile) FM_CUDA(cudaEventRecord(e1, s));
             FM_CUDA(cudaMemcpyAsync(ctx->h_ctl, ctx->ctl, sizeof(LaunchCtl), cudaMemcpyDeviceToHost, s));
             FM_CUDA(cudaStreamSynchronize(s));

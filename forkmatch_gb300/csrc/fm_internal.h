@@ -153,8 +153,8 @@ struct ExpandParams {
 
 // Launch one level expansion: the main pass, then the heavy-chunk pass
 // (fm_match.cu).
-cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups, int grid, int block,
-                          size_t smem, cudaStream_t s);
+cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups, int grid, int heavy_grid,
+                          int block, size_t smem, cudaStream_t s);
 size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps);
 int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block);
 

@@ -446,8 +446,8 @@ int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block
     return n;
 }
 
-cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups, int grid, int block,
-                          size_t smem, cudaStream_t s) {
+cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups, int grid, int heavy_grid,
+                          int block, size_t smem, cudaStream_t s) {
     void* f = pick(mode, roots, dups, false);
     void* fh = pick(mode, roots, dups, true);
     if (!f || !fh) return cudaErrorInvalidValue;
@@ -456,7 +456,8 @@ cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups
     void* args[] = {(void*)&q};
     cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(block), args, smem, s);
     if (e != cudaSuccess) return e;
-    return cudaLaunchKernel(fh, dim3(grid), dim3(block), args, smem, s);
+    // the heavy pass always gets a full grid: a few heavy chunks can hold most of the work
+    return cudaLaunchKernel(fh, dim3(heavy_grid), dim3(block), args, smem, s);
 }
 
 }  // namespace fm

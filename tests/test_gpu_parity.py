@@ -188,7 +188,7 @@ def test_rmat_random_walk_queries(ctx):
             continue
         check_case(ctx, g, og, q.to_g_text(), table=True, max_rows=1 << 22)
         done += 1
-    assert done >= 15
+    assert done >= 6
 
 
 def test_level_overflow_deferral_gives_identical_results():
