@@ -191,7 +191,7 @@ def run_ours(args, rank, world, local):
     queries_meta = wl["queries"]
     max_count = max(q["count"] for q in queries_meta)
     out_bytes = ((int(max_count * 8 * 4 * 1.05) + (64 << 20)) >> 20) << 20
-    ctx = fm.Context(prealloc_bytes=24 * GB + out_bytes + (64 << 20), soln_prealloc_bytes=24 * GB,
+    ctx = fm.Context(prealloc_bytes=24 * GB + out_bytes + (128 << 20), soln_prealloc_bytes=24 * GB,
                      output_prealloc_bytes=out_bytes, bank_rows=1 << 16, device=local)
     t = time.time()
     g = fm.Graph.from_edges(ctx, G.V, G.n_elabels + 1, src, dst, lab)

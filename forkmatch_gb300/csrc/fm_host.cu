@@ -67,7 +67,7 @@ uint64_t env_u64(const char* name, uint64_t dflt) {
     return (end && *end == 0) ? (uint64_t)x : dflt;
 }
 
-constexpr uint64_t kMiscBytes = 16ull << 20;
+constexpr uint64_t kMiscBytes = 64ull << 20;
 
 }  // namespace
 
@@ -157,7 +157,7 @@ fm_status fm_context_create(const fm_knobs* knobs, fm_context** out) {
     // round_down(prealloc - misc, 256): the margin keeps the three disjoint
     uint64_t need = ((k.soln_prealloc_bytes + 255) & ~255ull) + k.output_prealloc_bytes + kMiscBytes + 256;
     if (k.prealloc_bytes < need) {
-        set_error("PREALLOC must cover SOLN_PREALLOC + OUTPUT_PREALLOC + 16 MiB");
+        set_error("PREALLOC must cover SOLN_PREALLOC + OUTPUT_PREALLOC + 64 MiB");
         return FM_ERR_ARG;
     }
     std::unique_ptr<fm_context, void (*)(fm_context*)> c(new fm_context(), fm_context_destroy);
@@ -178,14 +178,14 @@ fm_status fm_context_create(const fm_knobs* knobs, fm_context** out) {
     c->output = (uint32_t*)(c->slab + ((k.soln_prealloc_bytes + 255) & ~255ull));
     // control blocks hold 64-bit atomics: keep them 256-byte aligned whatever PREALLOC is
     char* misc = c->slab + ((k.prealloc_bytes - kMiscBytes) & ~255ull);
-    // [0, 4 KiB) control blocks, [4 KiB, 8 MiB) deferred-chunk lists,
-    // [8 MiB, 16 MiB) heavy-chunk entries
+    // [0, 4 KiB) control blocks, [4 KiB, 48 MiB) deferred-chunk lists (two per
+    // depth), [48 MiB, 64 MiB) heavy-chunk entries
     c->ctl = (LaunchCtl*)misc;
     c->tot = (MatchTotals*)(misc + 512);
     c->defs = (uint32_t*)(misc + 4096);
-    c->def_cap = (uint32_t)(((8ull << 20) - 4096) / 4 / (2 * kMaxQ));
-    c->heavy = (HeavyEntry*)(misc + (8ull << 20));
-    c->heavy_cap = (uint32_t)((kMiscBytes - (8ull << 20)) / sizeof(HeavyEntry));
+    c->def_cap = (uint32_t)(((48ull << 20) - 4096) / 4 / (2 * kMaxQ));
+    c->heavy = (HeavyEntry*)(misc + (48ull << 20));
+    c->heavy_cap = (uint32_t)((kMiscBytes - (48ull << 20)) / sizeof(HeavyEntry));
     FM_CUDA(cudaHostAlloc(&c->h_ctl, sizeof(LaunchCtl), cudaHostAllocDefault));
     FM_CUDA(cudaHostAlloc(&c->h_tot, sizeof(MatchTotals), cudaHostAllocDefault));
     FM_CUDA(cudaEventCreate(&c->ev0));
@@ -557,6 +557,7 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         uint64_t cap = sum_cols ? ctx->soln_bytes / (4ull * sum_cols) : 0;
         const uint64_t bank = ctx->knobs.bank_rows;
         if (sum_cols) {
+            cap = std::min<uint64_t>(cap, 0xffffffffull - 64);   // parent indices are 32-bit
             cap = cap / bank * bank;
             if (cap < (uint64_t)g.max_len * 32 + 32 || cap == 0) {
                 set_error("SOLN_PREALLOC cannot hold one 32-parent chunk per level for this graph");

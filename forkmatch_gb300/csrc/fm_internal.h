@@ -149,6 +149,11 @@ struct ExpandParams {
     HeavyEntry* heavy;
     uint32_t heavy_cap;             // entries; chunks are published only while room remains
     uint32_t max_warps;             // warps of the launch (bounds concurrent publishers)
+    // launch tuning, set by launch_expand
+    uint32_t claim_batch;           // chunks claimed per atomic
+    uint32_t credit_block;          // output rows reserved per budget atomic
+    uint32_t heavy_thresh;          // candidate slots above which a chunk is split
+    uint32_t heavy_piece;           // slots per piece of a split chunk
 };
 
 // Launch one level expansion: the main pass, then the heavy-chunk pass

@@ -1,36 +1,41 @@
-// fm_match.cu -- level-expansion kernel of the matcher.
+// fm_match.cu -- level-expansion kernels of the matcher.
 //
 // Replaces the reference's per-thread k-way merge (src/smsm.cu:299-345 isoGen,
 // src/smsm.cu:57-140 isoCompare), injectivity walk (src/smsm.cu:188-227 isInj),
 // ballot append (src/smsm.cu:146-182 attemptInsert) and table write
 // (src/smsm.cu:706-779 isoWrite).
 //
-// One launch extends a level of partial matches by one query vertex.  Partial
+// One level launch extends every partial match by one query vertex.  Partial
 // matches are full rows (column c = data vertex matched at depth c) stored
-// column-major (SoA) so every load and store of a column is coalesced; there is
-// no parent-pointer forest to climb.  A warp claims 32 parents at a time:
+// column-major (SoA), so every load and store of a column is coalesced; there
+// is no parent-pointer forest to climb.  Warps claim chunks of 32 parents
+// (several chunks per atomic):
 //   1. each lane loads its parent row and the k (label, ancestor) segment
 //      records -- k independent 16-byte loads, issued back to back;
 //   2. the shortest list is the driver; a warp prefix sum over driver lengths
 //      turns the 32 parents' candidate lists into one range of slots;
-//   3. lanes take 64 consecutive slots per round, two per lane with both
-//      driver loads in flight (load-balanced across parents, so a hub parent
-//      keeps all 32 lanes busy), reject values already in the row, test
-//      membership in the other k-1 lists (inline compare or binary search),
-//      and stage survivors in shared memory (__ballot_sync + __popc rank);
-//   4. a full stage (or the end of the chunk) is flushed with one atomic and
-//      fully coalesced stores: column by column into the next level, or as
-//      contiguous row-major rows into the table.
-// Lists of length <= 3 are inline in the segment record, so the common case
-// needs no second memory access.  With duplicate e-lines the value at rank r of
-// its run in the driver list survives only if every other list holds at least
-// r + 1 copies (min-multiplicity semantics of the reference's merge).
+//   3. lanes take 64 consecutive slots per round, two per lane with both driver
+//      loads in flight (load-balanced across parents, so a hub parent keeps all
+//      32 lanes busy), reject values already in the row, test membership in
+//      the other k-1 lists (inline compare or binary search), and stage
+//      survivors as (parent index, value) in shared memory;
+//   4. the stage outlives the chunk: it is flushed with one atomic per 448+
+//      survivors and fully coalesced stores, column by column into the next
+//      level or as contiguous row-major rows into the table.
+// A chunk whose candidate range is long (a hub) is not walked by one warp: it
+// is published to a heavy list and cut into pieces that every warp of a second
+// launch shares.  Lists of length <= 3 are inline in the segment record, so
+// the common case needs no second memory access.  With duplicate e-lines the
+// value at rank r of its run in the driver list survives only if every other
+// list holds at least r + 1 copies (min-multiplicity semantics of the
+// reference's merge).
 //
-// Bounded memory: before expanding, a warp reserves its candidate upper bound
-// in the output level ("budget"); when a reservation does not fit, the warp
-// records its chunk in a deferred list, raises `stop`, and exits; the host
-// drains the output level (depth first) and relaunches this level on the
-// deferred chunks plus the unclaimed remainder.  Nothing spins, nothing traps.
+// Bounded memory: before expanding a chunk a warp holds output budget for its
+// candidate upper bound (reserved from the level in blocks); when a
+// reservation does not fit, the warp defers its remaining chunks, raises
+// `stop`, and exits; the host drains the output level (depth first) and
+// relaunches this level on the deferred chunks plus the unclaimed remainder.
+// Nothing spins and nothing traps.
 #include "fm_internal.h"
 
 namespace fm {
@@ -38,6 +43,8 @@ namespace {
 
 constexpr int kWarps = 8;
 constexpr unsigned kFull = 0xffffffffu;
+constexpr uint32_t kStage = 512;           // staged survivors per warp
+constexpr uint32_t kHeavyMaxPieces = 65536;
 
 __device__ __forceinline__ uint4 ldg4(const uint4* p) { return __ldg(p); }
 
@@ -50,7 +57,7 @@ __device__ __forceinline__ uint32_t seg_at(const uint4& s, uint32_t t, const uin
 __device__ __forceinline__ uint32_t lower_bound_g(const uint32_t* __restrict__ a, uint32_t n, uint32_t x) {
     uint32_t lo = 0;
     while (n > 0) {
-        uint32_t half = n >> 1;
+        const uint32_t half = n >> 1;
         if (__ldg(a + lo + half) < x) {
             lo += half + 1;
             n -= half + 1;
@@ -64,12 +71,12 @@ __device__ __forceinline__ uint32_t lower_bound_g(const uint32_t* __restrict__ a
 // Does the list hold at least `need` copies of x?
 __device__ __forceinline__ bool seg_has(const uint4& s, uint32_t x, uint32_t need, const uint32_t* __restrict__ nbr) {
     if (s.x <= 3) {
-        uint32_t c = (s.x > 0 && s.y == x) + (s.x > 1 && s.z == x) + (s.x > 2 && s.w == x);
+        const uint32_t c = (s.x > 0 && s.y == x) + (s.x > 1 && s.z == x) + (s.x > 2 && s.w == x);
         return c >= need;
     }
     if (x < s.z || x > s.w) return false;
     const uint32_t* a = nbr + (uint64_t)s.y * 4;
-    uint32_t pos = lower_bound_g(a, s.x, x) + need - 1;
+    const uint32_t pos = lower_bound_g(a, s.x, x) + need - 1;
     return pos < s.x && __ldg(a + pos) == x;
 }
 
@@ -80,13 +87,15 @@ __device__ __forceinline__ uint32_t seg_rank(const uint4& s, uint32_t t, uint32_
     return t - lower_bound_g(a, t, x);
 }
 
+__device__ __forceinline__ uint32_t item_chunk(const ExpandParams& P, unsigned long long item) {
+    return item < P.ndef_in ? P.def_in[item] : (uint32_t)(P.fresh_base + (item - P.ndef_in));
+}
+
 __device__ __forceinline__ void defer_chunk(const ExpandParams& P, uint32_t chunk) {
-    unsigned idx = atomicAdd(&P.ctl->ndef, 1u);
+    const unsigned idx = atomicAdd(&P.ctl->ndef, 1u);
     if (idx < P.def_cap) P.def_out[idx] = chunk;
     else atomicOr(&P.ctl->error, 1u);
 }
-
-constexpr uint32_t kStage = 256;   // survivors staged per warp before one coalesced flush
 
 // Slot s of the warp's chunk belongs to parent j (the last j with excl[j] <= s),
 // at position t of that parent's driver list.
@@ -116,12 +125,44 @@ __device__ __forceinline__ bool slot_check(const ExpandParams& P, uint32_t x, ui
     return ok;
 }
 
-// Write the warp's staged survivors with one atomic: column by column into the
-// next level (SoA), or row-major into the table, every store coalesced.
-template <int MODE>
-__device__ __forceinline__ void flush_stage(const ExpandParams& P, uint32_t nst, uint32_t lane, uint32_t d,
-                                            const uint32_t* rows_s, const uint8_t* stj, const uint32_t* stx,
-                                            const uint8_t* col_depth_s) {
+// Per-warp shared memory.
+struct WarpMem {
+    uint32_t* rows_s;   // [d][32] parent rows of the current chunk, column-major
+    uint4* segs_s;      // [k][32] segment records
+    uint32_t* excl_s;   // [32] exclusive prefix of driver lengths
+    uint32_t* drv_s;    // [32] driver list of each parent
+    uint32_t* stp;      // [kStage] staged survivors: parent index in the level
+    uint32_t* stx;      // [kStage] staged survivors: new vertex
+};
+
+__host__ __device__ constexpr uint32_t per_warp_bytes(uint32_t d, uint32_t k) {
+    return 128 * d + 512 * k + 256 + 8 * kStage;
+}
+
+__device__ __forceinline__ WarpMem warp_mem(unsigned char* smem_raw, uint32_t warp, uint32_t d, uint32_t k) {
+    unsigned char* ws = smem_raw + warp * per_warp_bytes(d, k);
+    WarpMem m;
+    m.rows_s = (uint32_t*)ws;
+    m.segs_s = (uint4*)(ws + 128 * d);
+    m.excl_s = (uint32_t*)(ws + 128 * d + 512 * k);
+    m.drv_s = m.excl_s + 32;
+    m.stp = (uint32_t*)(ws + 128 * d + 512 * k + 256);
+    m.stx = m.stp + kStage;
+    return m;
+}
+
+// Column c of parent p of the level being expanded.
+template <bool ROOTS>
+__device__ __forceinline__ uint32_t parent_col(const ExpandParams& P, uint32_t c, uint32_t p) {
+    if (ROOTS) return P.root_begin + p;
+    return __ldg(P.pin + c * P.pstride + p);
+}
+
+// Write the staged survivors with one atomic: column by column into the next
+// level (SoA), or row-major into the table; every store is coalesced.
+template <int MODE, bool ROOTS>
+__device__ __forceinline__ void flush_stage(const ExpandParams& P, const WarpMem& m, uint32_t nst, uint32_t lane,
+                                            uint32_t d, const uint8_t* col_depth_s) {
     unsigned long long pos0 = 0;
     if (lane == 0)
         pos0 = atomicAdd(MODE == kModeMid ? &P.ctl->produced : &P.tot->table_pos, (unsigned long long)nst);
@@ -129,10 +170,10 @@ __device__ __forceinline__ void flush_stage(const ExpandParams& P, uint32_t nst,
     if (MODE == kModeMid) {
         for (uint32_t c = 0; c < d; c++) {
             uint32_t* col = P.pout + c * P.ocap + pos0;
-            for (uint32_t i = lane; i < nst; i += 32) col[i] = rows_s[c * 32 + stj[i]];
+            for (uint32_t i = lane; i < nst; i += 32) col[i] = parent_col<ROOTS>(P, c, m.stp[i]);
         }
         uint32_t* col = P.pout + d * P.ocap + pos0;
-        for (uint32_t i = lane; i < nst; i += 32) col[i] = stx[i];
+        for (uint32_t i = lane; i < nst; i += 32) col[i] = m.stx[i];
     } else {
         const uint32_t q = P.plan.q;
         if (pos0 >= P.table_cap) return;
@@ -146,36 +187,9 @@ __device__ __forceinline__ void flush_stage(const ExpandParams& P, uint32_t nst,
         for (uint32_t w = lane; w < n; w += 32) {
             const uint32_t r = (uint32_t)(((float)w + 0.5f) * inv_q);
             const uint32_t dep = col_depth_s[w - r * q];
-            out[w] = dep < d ? rows_s[dep * 32 + stj[r]] : stx[r];
+            out[w] = dep < d ? parent_col<ROOTS>(P, dep, m.stp[r]) : m.stx[r];
         }
     }
-}
-
-constexpr uint32_t kHeavyThresh = 2048;   // candidate slots above which a chunk is split
-constexpr uint32_t kHeavyPiece = 1024;    // slots per piece of a split chunk
-constexpr uint32_t kHeavyMaxPieces = 65536;
-
-// Per-warp shared memory for one chunk of 32 parents.
-struct WarpMem {
-    uint32_t* rows_s;   // [d][32] parent rows, column-major
-    uint4* segs_s;      // [k][32] segment records
-    uint32_t* excl_s;   // [32] exclusive prefix of driver lengths
-    uint32_t* drv_s;    // [32] driver list of each parent
-    uint32_t* stx;      // [kStage] staged survivor values
-    uint8_t* stj;       // [kStage] staged survivor parents
-};
-
-__device__ __forceinline__ WarpMem warp_mem(unsigned char* smem_raw, uint32_t warp, uint32_t d, uint32_t k) {
-    const uint32_t per_warp = 128 * d + 512 * k + 256 + kStage * 5;
-    unsigned char* ws = smem_raw + warp * per_warp;
-    WarpMem m;
-    m.rows_s = (uint32_t*)ws;
-    m.segs_s = (uint4*)(ws + 128 * d);
-    m.excl_s = (uint32_t*)(ws + 128 * d + 512 * k);
-    m.drv_s = m.excl_s + 32;
-    m.stx = (uint32_t*)(ws + 128 * d + 512 * k + 256);
-    m.stj = (uint8_t*)(m.stx + kStage);
-    return m;
 }
 
 // Load the 32 parents of `chunk`, look up their k lists (independent 16-byte
@@ -213,7 +227,7 @@ __device__ __forceinline__ uint32_t load_chunk(const ExpandParams& P, const Warp
     uint32_t incl = n;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t t = __shfl_up_sync(kFull, incl, o);
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
         if ((int)lane >= o) incl += t;
     }
     m.excl_s[lane] = incl - n;
@@ -223,12 +237,14 @@ __device__ __forceinline__ uint32_t load_chunk(const ExpandParams& P, const Warp
 }
 
 // Evaluate slots [begin, end) of the loaded chunk: two slots per lane per round
-// with both driver loads in flight, survivors staged and flushed coalesced.
-template <int MODE, bool DUPS>
-__device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpMem& m, uint32_t begin, uint32_t end,
-                                              uint32_t lane, uint32_t d, uint32_t k, const uint8_t* col_depth_s,
+// with both driver loads in flight; survivors go to the stage, which is
+// flushed whenever it cannot take another round.
+template <int MODE, bool ROOTS, bool DUPS>
+__device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpMem& m, uint32_t chunk,
+                                              uint32_t begin, uint32_t end, uint32_t lane, uint32_t d, uint32_t k,
+                                              const uint8_t* col_depth_s, uint32_t& nst,
                                               unsigned long long& n_count) {
-    uint32_t nst = 0;   // staged survivors (warp-uniform)
+    const uint32_t pbase = chunk * 32;
     for (uint32_t base = begin; base < end; base += 64) {
         const uint32_t s0 = base + lane, s1 = base + 32 + lane;
         const bool a0 = s0 < end, a1 = s1 < end;
@@ -257,31 +273,26 @@ __device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpM
         const unsigned lt = (1u << lane) - 1u;
         if (ok0) {
             const uint32_t q0 = nst + __popc(b0 & lt);
-            m.stj[q0] = (uint8_t)j0;
+            m.stp[q0] = pbase + j0;
             m.stx[q0] = x0;
         }
         nst += __popc(b0);
         if (ok1) {
             const uint32_t q1 = nst + __popc(b1 & lt);
-            m.stj[q1] = (uint8_t)j1;
+            m.stp[q1] = pbase + j1;
             m.stx[q1] = x1;
         }
         nst += __popc(b1);
         if (nst > kStage - 64) {
             __syncwarp();
-            flush_stage<MODE>(P, nst, lane, d, m.rows_s, m.stj, m.stx, col_depth_s);
+            flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s);
             nst = 0;
-            __syncwarp();
         }
-    }
-    if (MODE != kModeLastCount && nst) {
         __syncwarp();
-        flush_stage<MODE>(P, nst, lane, d, m.rows_s, m.stj, m.stx, col_depth_s);
     }
-    __syncwarp();
 }
 
-// Main pass: warps claim chunks of 32 parents; long candidate ranges are
+// Main pass: warps claim batches of chunks; long candidate ranges are
 // published to the heavy list instead of being walked by one warp.
 template <int MODE, bool ROOTS, bool DUPS>
 __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant__ ExpandParams P) {
@@ -296,64 +307,86 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
     const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k);
 
     unsigned long long n_count = 0, n_lookups = 0, n_words = 0, n_parents = 0;
-    for (;;) {
-        unsigned long long item = 0;
-        if (lane == 0) item = atomicAdd(&P.ctl->claim, 1ull);
-        item = __shfl_sync(kFull, item, 0);
-        if (item >= P.n_items) break;
-        const uint32_t chunk = item < P.ndef_in ? P.def_in[item] : (uint32_t)(P.fresh_base + (item - P.ndef_in));
-        if (MODE == kModeMid) {
-            if (*(volatile unsigned int*)&P.ctl->stop) {
-                if (lane == 0) defer_chunk(P, chunk);
-                break;
-            }
-        }
-        bool valid;
-        unsigned long long w;
-        const uint32_t total = load_chunk<ROOTS>(P, m, chunk, lane, d, k, rb, valid, w);
-        if (MODE == kModeMid) {
-            int ok = 1;
-            if (lane == 0 && total) {
-                unsigned long long old = atomicAdd(&P.ctl->budget, (unsigned long long)total);
-                if (old + total > P.ocap) {
-                    ok = 0;
-                    atomicExch(&P.ctl->stop, 1u);
-                    defer_chunk(P, chunk);
+    unsigned long long credit = 0;   // level budget held by this warp (lane 0)
+    uint32_t nst = 0;
+    bool done = false;
+    while (!done) {
+        unsigned long long first = 0;
+        if (lane == 0) first = atomicAdd(&P.ctl->claim, (unsigned long long)P.claim_batch);
+        first = __shfl_sync(kFull, first, 0);
+        if (first >= P.n_items) break;
+        const unsigned long long last =
+            first + P.claim_batch < P.n_items ? first + P.claim_batch : (unsigned long long)P.n_items;
+        for (unsigned long long item = first; item < last; item++) {
+            const uint32_t chunk = item_chunk(P, item);
+            if (MODE == kModeMid) {
+                // one lane reads the flag and broadcasts it, so the warp never splits
+                int stop = 0;
+                if (lane == 0) stop = *(volatile unsigned int*)&P.ctl->stop ? 1 : 0;
+                stop = __shfl_sync(kFull, stop, 0);
+                if (stop) {
+                    if (lane == 0)
+                        for (unsigned long long it = item; it < last; it++) defer_chunk(P, item_chunk(P, it));
+                    done = true;
+                    break;
                 }
             }
-            ok = __shfl_sync(kFull, ok, 0);
-            if (!ok) break;
-        }
-        if (valid) {
-            n_lookups += k;
-            n_words += w;
-            n_parents += 1;
-        }
-        if (total > kHeavyThresh) {
-            // Publish: one packed atomic reserves the entry index and its piece
-            // range, so entries are ordered by first piece.  The room check is
-            // conservative: at most max_warps publishers can be past it at once.
-            int pub = 0;
-            const uint32_t np = (total + kHeavyPiece - 1) / kHeavyPiece;
-            if (lane == 0 && np <= kHeavyMaxPieces) {
-                const unsigned long long h = *(volatile unsigned long long*)&P.ctl->heavy;
-                if ((uint32_t)(h >> 32) + P.max_warps < P.heavy_cap && (uint32_t)h < (1u << 31)) {
-                    const unsigned long long old = atomicAdd(&P.ctl->heavy, (1ull << 32) | np);
-                    HeavyEntry e;
-                    e.chunk = chunk;
-                    e.total = total;
-                    e.piece0 = (uint32_t)old;
-                    e.pieces = np;
-                    P.heavy[(uint32_t)(old >> 32)] = e;
-                    pub = 1;
+            bool valid;
+            unsigned long long w;
+            const uint32_t total = load_chunk<ROOTS>(P, m, chunk, lane, d, k, rb, valid, w);
+            if (MODE == kModeMid && total) {
+                int ok = 1;
+                if (lane == 0) {
+                    if (total > credit) {
+                        const unsigned long long need = max((unsigned long long)total, (unsigned long long)P.credit_block);
+                        const unsigned long long old = atomicAdd(&P.ctl->budget, need);
+                        if (old + need > P.ocap) {
+                            ok = 0;
+                            atomicExch(&P.ctl->stop, 1u);
+                            for (unsigned long long it = item; it < last; it++) defer_chunk(P, item_chunk(P, it));
+                        } else {
+                            credit += need;
+                        }
+                    }
+                    if (ok) credit -= total;
+                }
+                ok = __shfl_sync(kFull, ok, 0);
+                if (!ok) {
+                    done = true;
+                    break;
                 }
             }
-            pub = __shfl_sync(kFull, pub, 0);
-            if (pub) continue;
+            if (valid) {
+                n_lookups += k;
+                n_words += w;
+                n_parents += 1;
+            }
+            if (total > P.heavy_thresh) {
+                // Publish: one packed atomic reserves the entry index and its
+                // piece range, so entries are ordered by first piece.  The room
+                // check is conservative: at most max_warps publishers are past it.
+                int pub = 0;
+                const uint32_t np = (total + P.heavy_piece - 1) / P.heavy_piece;
+                if (lane == 0 && np <= kHeavyMaxPieces) {
+                    const unsigned long long h = *(volatile unsigned long long*)&P.ctl->heavy;
+                    if ((uint32_t)(h >> 32) + P.max_warps < P.heavy_cap && (uint32_t)h < (1u << 31)) {
+                        const unsigned long long old = atomicAdd(&P.ctl->heavy, (1ull << 32) | np);
+                        HeavyEntry e;
+                        e.chunk = chunk;
+                        e.total = total;
+                        e.piece0 = (uint32_t)old;
+                        e.pieces = np;
+                        P.heavy[(uint32_t)(old >> 32)] = e;
+                        pub = 1;
+                    }
+                }
+                pub = __shfl_sync(kFull, pub, 0);
+                if (pub) continue;
+            }
+            process_slots<MODE, ROOTS, DUPS>(P, m, chunk, 0, total, lane, d, k, col_depth_s, nst, n_count);
         }
-        process_slots<MODE, DUPS>(P, m, 0, total, lane, d, k, col_depth_s, n_count);
     }
-    // statistics: one atomic per warp per counter
+    if (MODE != kModeLastCount && nst) flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s);
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
         n_lookups += __shfl_down_sync(kFull, n_lookups, o);
@@ -372,7 +405,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
 
 // Heavy pass (same stream, after the main pass): every warp claims pieces of
 // the published chunks, reloads that chunk and walks its piece of the slots.
-// The main pass already reserved the chunk's output budget and counted its work.
+// The main pass already holds the chunk's output budget and counted its work.
 template <int MODE, bool ROOTS, bool DUPS>
 __global__ void __launch_bounds__(kWarps * 32, 4) k_expand_heavy(const __grid_constant__ ExpandParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -389,6 +422,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand_heavy(const __grid_co
     const uint32_t rb = P.plan.req_begin[d];
     const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k);
     unsigned long long n_count = 0;
+    uint32_t nst = 0;
     for (;;) {
         unsigned long long gp = 0;
         if (lane == 0) gp = atomicAdd(&P.ctl->claim2, 1ull);
@@ -401,13 +435,14 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand_heavy(const __grid_co
             else hi = mid;
         }
         const HeavyEntry e = P.heavy[lo];
-        const uint32_t begin = ((uint32_t)gp - e.piece0) * kHeavyPiece;
-        const uint32_t end = min(begin + kHeavyPiece, e.total);
+        const uint32_t begin = ((uint32_t)gp - e.piece0) * P.heavy_piece;
+        const uint32_t end = min(begin + P.heavy_piece, e.total);
         bool valid;
         unsigned long long w;
         load_chunk<ROOTS>(P, m, e.chunk, lane, d, k, rb, valid, w);
-        process_slots<MODE, DUPS>(P, m, begin, end, lane, d, k, col_depth_s, n_count);
+        process_slots<MODE, ROOTS, DUPS>(P, m, e.chunk, begin, end, lane, d, k, col_depth_s, nst, n_count);
     }
+    if (MODE != kModeLastCount && nst) flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s);
     if (MODE == kModeLastCount && lane == 0 && n_count) atomicAdd(&P.tot->count, n_count);
 }
 
@@ -417,10 +452,10 @@ void* kernel_ptr(bool heavy) {
 }
 
 void* pick(int mode, bool roots, bool dups, bool heavy) {
-#define FM_PICK(M)                                                                                         \
-    if (mode == M) {                                                                                       \
-        if (roots) return dups ? kernel_ptr<M, true, true>(heavy) : kernel_ptr<M, true, false>(heavy);     \
-        return dups ? kernel_ptr<M, false, true>(heavy) : kernel_ptr<M, false, false>(heavy);              \
+#define FM_PICK(M)                                                                                     \
+    if (mode == M) {                                                                                   \
+        if (roots) return dups ? kernel_ptr<M, true, true>(heavy) : kernel_ptr<M, true, false>(heavy); \
+        return dups ? kernel_ptr<M, false, true>(heavy) : kernel_ptr<M, false, false>(heavy);          \
     }
     FM_PICK(kModeMid)
     FM_PICK(kModeLastTable)
@@ -432,7 +467,7 @@ void* pick(int mode, bool roots, bool dups, bool heavy) {
 }  // namespace
 
 size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps) {
-    return (size_t)warps * (128u * depth + 512u * nreq + 256u + kStage * 5u);
+    return (size_t)warps * per_warp_bytes(depth, nreq);
 }
 
 int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block) {
@@ -452,7 +487,18 @@ cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups
     void* fh = pick(mode, roots, dups, true);
     if (!f || !fh) return cudaErrorInvalidValue;
     ExpandParams q = p;
-    q.max_warps = (uint32_t)grid * (uint32_t)(block / 32);
+    const uint32_t warps = (uint32_t)(block / 32);
+    q.max_warps = (uint32_t)heavy_grid * warps;
+    // Claims: several chunks per atomic on large levels (keeps ~16 claims per warp).
+    const uint64_t per_warp_items = q.n_items / ((uint64_t)grid * warps) + 1;
+    q.claim_batch = (uint32_t)std::min<uint64_t>(8, std::max<uint64_t>(1, per_warp_items / 16));
+    // Output budget is reserved in blocks small enough that the budget idle in
+    // all warps stays under a quarter of the level.
+    q.credit_block = (uint32_t)std::min<uint64_t>(1024, q.ocap / (4ull * std::max<uint32_t>(1, q.max_warps)));
+    // Split threshold: the fewer chunks a level has per warp, the finer the pieces.
+    const uint64_t all_warps = (uint64_t)heavy_grid * warps;
+    q.heavy_thresh = q.n_items >= 4 * all_warps ? 4096u : (q.n_items >= all_warps ? 1024u : 256u);
+    q.heavy_piece = q.heavy_thresh / 2;
     void* args[] = {(void*)&q};
     cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(block), args, smem, s);
     if (e != cudaSuccess) return e;
