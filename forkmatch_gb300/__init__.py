@@ -64,7 +64,7 @@ class MatchOpts(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("columns", ctypes.c_int32), ("stream", ctypes.c_void_p),
                 ("host_rows", ctypes.c_void_p), ("host_rows_cap", ctypes.c_uint64),
                 ("root_begin", ctypes.c_uint32), ("root_end", ctypes.c_uint32), ("profile", ctypes.c_int32),
-                ("order", ctypes.c_int32)]
+                ("order", ctypes.c_int32), ("host_direct", ctypes.c_int32)]
 
 
 class LevelStats(ctypes.Structure):
@@ -266,15 +266,18 @@ class PinnedRows:
 
 
 def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_rows=None, roots=None,
-          profile=False, stream=None, allow_truncation=False, order=ORDER_AUTO):
+          profile=False, stream=None, allow_truncation=False, order=ORDER_AUTO, host_direct=False):
     """Run fm_match.  Returns the Result struct; with ``host_rows`` (a
-    PinnedRows or a C-contiguous uint32 numpy array) the table is copied there."""
+    PinnedRows or a C-contiguous uint32 numpy array) the table is copied there.
+    ``host_direct`` (PinnedRows only): the kernels write the table straight
+    into the pinned host buffer instead of device memory."""
     o = MatchOpts()
     lib().fm_match_opts_default(ctypes.byref(o))
     o.mode = mode
     o.columns = columns
     o.profile = 1 if profile else 0
     o.order = order
+    o.host_direct = 1 if host_direct else 0
     if stream is not None:
         o.stream = stream
     if roots is not None:

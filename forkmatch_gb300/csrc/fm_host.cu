@@ -124,7 +124,11 @@ void fm_match_opts_default(fm_match_opts* o) {
 
 void* fm_host_alloc(uint64_t bytes) {
     void* p = nullptr;
-    if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+    // mapped + portable: the kernels of any context can write it directly (host_direct)
+    if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
     return p;
 }
 
@@ -491,7 +495,22 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     if (re > g.V) re = g.V;
     if (rb > re) rb = re;
     const bool table = opts.mode == FM_MODE_TABLE;
-    const uint64_t table_cap = ctx->output_bytes / (4ull * q);
+    // The table lives in the context's OUTPUT_PREALLOC region, or -- host_direct --
+    // in the caller's pinned host buffer, written by the kernels over the host link.
+    const bool direct = table && opts.host_direct && opts.host_rows;
+    uint32_t* table_ptr = ctx->output;
+    uint64_t table_cap = ctx->output_bytes / (4ull * q);
+    if (direct) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, opts.host_rows) != cudaSuccess || a.type != cudaMemoryTypeHost ||
+            !a.devicePointer) {
+            cudaGetLastError();
+            set_error("host_direct needs host_rows in pinned host memory (fm_host_alloc)");
+            return FM_ERR_ARG;
+        }
+        table_ptr = (uint32_t*)a.devicePointer;
+        table_cap = opts.host_rows_cap;
+    }
 
     // matching order: the reference's, or the cheapest one for this graph
     uint32_t order[kMaxQ];
@@ -547,7 +566,7 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     if (q == 1) {
         uint64_t n = re - rb;
         if (table && n) {
-            k_iota_rows<<<(unsigned)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(ctx->output, n, rb, table_cap);
+            k_iota_rows<<<(unsigned)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(table_ptr, n, rb, table_cap);
             FM_CUDA(cudaGetLastError());
         }
         out->count = n;
@@ -584,8 +603,9 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         b.nbr = g.nbr;
         b.V = g.V;
         b.root_begin = rb;
-        b.table = ctx->output;
+        b.table = table_ptr;
         b.table_cap = table_cap;
+        b.table_vec4 = (q % 4 == 0 && ((uintptr_t)table_ptr % 16) == 0) ? 1u : 0u;
         b.ctl = ctx->ctl;
         b.tot = ctx->tot;
         b.heavy = ctx->heavy;
@@ -602,9 +622,11 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     if (q > 1) out->count = table ? ctx->h_tot->table_pos : ctx->h_tot->count;
     out->rows = table ? std::min<uint64_t>(out->count, table_cap) : 0;
     out->truncated = table && out->count > table_cap;
-    out->rows_device = table ? ctx->output : nullptr;
+    out->rows_device = (table && !direct) ? ctx->output : nullptr;
     if (q > 1) out->level[q - 1].produced = out->count;
-    if (table && opts.host_rows && out->rows) {
+    if (direct) {
+        out->rows_copied = out->rows;   // already in host memory
+    } else if (table && opts.host_rows && out->rows) {
         uint64_t n = std::min<uint64_t>(out->rows, opts.host_rows_cap);
         FM_CUDA(cudaMemcpyAsync(opts.host_rows, ctx->output, n * q * 4, cudaMemcpyDeviceToHost, s));
         FM_CUDA(cudaStreamSynchronize(s));

@@ -142,8 +142,9 @@ struct ExpandParams {
     // outputs
     uint32_t* pout;                 // SoA, column c at pout + c*ocap
     uint64_t ocap;
-    uint32_t* table;                // rows of q
+    uint32_t* table;                // rows of q (device memory, or mapped pinned host memory)
     uint64_t table_cap;
+    uint32_t table_vec4;            // rows can be written as 16-byte vectors (q % 4 == 0, aligned)
     LaunchCtl* ctl;
     MatchTotals* tot;
     HeavyEntry* heavy;

@@ -175,19 +175,35 @@ __device__ __forceinline__ void flush_stage(const ExpandParams& P, const WarpMem
         uint32_t* col = P.pout + d * P.ocap + pos0;
         for (uint32_t i = lane; i < nst; i += 32) col[i] = m.stx[i];
     } else {
+        // one row per lane; the warp's rows are contiguous, so the vector
+        // stores of a round cover one block of 32 * 4q bytes
         const uint32_t q = P.plan.q;
         if (pos0 >= P.table_cap) return;
         const uint64_t room = P.table_cap - pos0;
         const uint32_t rows = nst < room ? nst : (uint32_t)room;
         uint32_t* out = P.table + pos0 * q;
-        const uint32_t n = rows * q;
-        // row = w / q in single precision: w < 2^14 and the fractional part of
-        // (w + 0.5) / q stays >= 1/64 away from an integer, so it is exact
-        const float inv_q = 1.0f / (float)q;
-        for (uint32_t w = lane; w < n; w += 32) {
-            const uint32_t r = (uint32_t)(((float)w + 0.5f) * inv_q);
-            const uint32_t dep = col_depth_s[w - r * q];
-            out[w] = dep < d ? parent_col<ROOTS>(P, dep, m.stp[r]) : m.stx[r];
+        for (uint32_t r = lane; r < rows; r += 32) {
+            const uint32_t p = m.stp[r], x = m.stx[r];
+            uint32_t* o = out + (uint64_t)r * q;
+            if (P.table_vec4) {
+                for (uint32_t c = 0; c < q; c += 4) {
+                    uint4 v;
+                    uint32_t dep = col_depth_s[c];
+                    v.x = dep < d ? parent_col<ROOTS>(P, dep, p) : x;
+                    dep = col_depth_s[c + 1];
+                    v.y = dep < d ? parent_col<ROOTS>(P, dep, p) : x;
+                    dep = col_depth_s[c + 2];
+                    v.z = dep < d ? parent_col<ROOTS>(P, dep, p) : x;
+                    dep = col_depth_s[c + 3];
+                    v.w = dep < d ? parent_col<ROOTS>(P, dep, p) : x;
+                    *(uint4*)(o + c) = v;
+                }
+            } else {
+                for (uint32_t c = 0; c < q; c++) {
+                    const uint32_t dep = col_depth_s[c];
+                    o[c] = dep < d ? parent_col<ROOTS>(P, dep, p) : x;
+                }
+            }
         }
     }
 }

@@ -159,6 +159,9 @@ typedef struct fm_match_opts {
     uint32_t root_end;          /*   root_end == 0 means all vertices */
     int32_t profile;            /* 1: time every expansion launch with CUDA events */
     int32_t order;              /* fm_order: matching order used internally */
+    int32_t host_direct;        /* 1: the kernels write the table straight into host_rows over
+                                   the host link (host_rows must be pinned, e.g. fm_host_alloc);
+                                   no device copy of the table is kept */
 } fm_match_opts;
 
 /* Matching order.  Results (count, row set, column layout) do not depend on

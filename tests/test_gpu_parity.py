@@ -255,6 +255,25 @@ def test_query_id_columns(ctx):
     assert all(len(set(r)) == qi.q for r in id_rows.tolist()[:1000])
 
 
+def test_host_direct_table_matches_device_table(ctx):
+    """Rows written straight into pinned host memory equal the device table."""
+    G = S.erdos_renyi(3000, 15000, seed=41, n_elabels=2)
+    src, dst, lab = G.directed()
+    g = fm.Graph.from_edges(ctx, G.V, 3, src, dst, lab)
+    for qq in (S.query_cycle(4, [1, 2, 1, 2]), S.query_path(5, [1, 1, 2, 2]), S.query_star(3, [1, 2])):
+        q = fm.Query.from_text(qq.to_g_text())
+        c1, rows1, _ = fm.match_table(ctx, g, q)
+        pinned = fm.PinnedRows(c1 + 8, q.q)
+        for _ in range(2):
+            r = fm.match(ctx, g, q, host_rows=pinned, host_direct=True)
+            assert r.count == c1 and r.rows_copied == c1 and r.rows_device is None
+            assert np.array_equal(sorted_rows(pinned.view(c1)), sorted_rows(rows1))
+        # a too-small host buffer truncates the table, the count stays exact
+        small = fm.PinnedRows(max(1, c1 // 3), q.q)
+        r = fm.match(ctx, g, q, host_rows=small, host_direct=True, allow_truncation=True)
+        assert r.count == c1 and r.truncated == (c1 > small.cap)
+
+
 def test_single_vertex_and_single_edge_queries(ctx):
     V, s, d, l = cycle_graph(50)
     g = fm.Graph.from_edges(ctx, V, 2, s, d, l)
