@@ -34,6 +34,7 @@ EXPORTS = [
     "fm_context_stream", "fm_graph_load_file", "fm_graph_load_text", "fm_graph_from_edges", "fm_graph_get_info",
     "fm_graph_free", "fm_query_compile_file", "fm_query_compile_text", "fm_query_get_info", "fm_query_free",
     "fm_match_opts_default", "fm_match", "fm_host_alloc", "fm_host_free", "fm_version", "fm_device_count",
+    "fm_match_static",
 ]
 
 
@@ -113,6 +114,7 @@ def lib():
         L.fm_host_alloc.argtypes = [u64]
         L.fm_host_alloc.restype = vp
         L.fm_host_free.argtypes = [vp]
+        L.fm_match_static.argtypes = [vp, vp, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64), vp]
         _lib = L
     return _lib
 
@@ -293,6 +295,19 @@ def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_ro
     st = lib().fm_match(ctx._h, graph._h, query._h, ctypes.byref(o), ctypes.byref(r))
     _check(st, "fm_match", allow=(FM_ERR_OUTPUT_OVERFLOW,) if allow_truncation else ())
     return r
+
+
+def match_static(graph, query, rows_device_ptr=None, rows_cap=0, stream=None, allow_truncation=False):
+    """fm_match_static: match with no device allocation (scratch in the
+    library's fixed static array).  ``rows_device_ptr`` is a device buffer of
+    ``rows_cap`` rows of q uint32 (None counts only).  Returns
+    (count, rows_written)."""
+    cnt = ctypes.c_uint64()
+    rows = ctypes.c_uint64()
+    st = lib().fm_match_static(graph._h, query._h, rows_device_ptr, int(rows_cap), ctypes.byref(cnt),
+                               ctypes.byref(rows), stream)
+    _check(st, "fm_match_static", allow=(FM_ERR_OUTPUT_OVERFLOW,) if allow_truncation else ())
+    return cnt.value, rows.value
 
 
 def match_table(ctx, graph, query, columns=COLUMNS_REFERENCE, max_rows=1 << 24, order=ORDER_AUTO):

@@ -201,6 +201,22 @@ typedef struct fm_result {
 fm_status fm_match(fm_context* ctx, const fm_graph* g, const fm_query* q,
                    const fm_match_opts* opts, fm_result* out);
 
+/* Matching that allocates nothing.  No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc at match time (an application whose
+ * own pool owns all device memory and forbids stray allocations, or a
+ * latency-critical loop that cannot afford an allocation).  All scratch lives
+ * in one fixed 64 MiB array in this library's device data; a query/graph pair
+ * whose partial matches do not fit is rejected with FM_ERR_POOL.  Inputs: a
+ * resident graph and a compiled query (q >= 2).  Outputs: *count_out, and --
+ * when rows_out is a device buffer of rows_cap rows -- the table in the
+ * reference column layout (*rows_written rows; FM_ERR_OUTPUT_OVERFLOW if it did
+ * not fit, the count stays exact).  rows_out == NULL counts only.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. */
+fm_status fm_match_static(const fm_graph* g, const fm_query* q, uint32_t* rows_out, uint64_t rows_cap,
+                          uint64_t* count_out, uint64_t* rows_written, void* stream);
+
 /* Pinned host memory helpers (cudaHostAlloc / cudaFreeHost). */
 void* fm_host_alloc(uint64_t bytes);
 void fm_host_free(void* p);
