@@ -42,11 +42,47 @@ UNIT = "embeddings/s"
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plain_at_scale")
+    ap.add_argument("--ncu-step", action="store_true",
+                    help="run one untimed step with small knobs (SOLN 2 GiB, OUTPUT 4.5 GiB) for ncu captures")
+    ap.add_argument("--queries", default="all", help="with --ncu-step: comma-separated query indices")
     return ap.parse_args()
+
+
+def run_ncu_step(args):
+    """One step of the workload with small knobs, for ncu captures (prints the
+    total count; every count is checked against the recorded one)."""
+    import forkmatch_gb300 as fm
+    wl, G, (src, dst, lab), same, _ = load_workload(args.workload)
+    ctx = fm.Context(prealloc_bytes=7 * GB, soln_prealloc_bytes=2 * GB, output_prealloc_bytes=int(4.5 * GB),
+                     bank_rows=1 << 12)
+    g = fm.Graph.from_edges(ctx, G.V, G.n_elabels + 1, src, dst, lab)
+    pick = None if args.queries == "all" else {int(x) for x in args.queries.split(",")}
+    tot = 0
+    for i, qm in enumerate(wl["queries"]):
+        if pick is not None and i not in pick:
+            continue
+        r = fm.match(ctx, g, fm.Query.from_text(qm["text"].encode()), mode=fm.MODE_TABLE)
+        if same and r.count != qm["count"]:
+            raise SystemExit("count mismatch on query %d: %d != %d" % (i, r.count, qm["count"]))
+        tot += r.count
+    print("ncu step ok", tot)
+    return 0
+
+
+def profiled_traffic():
+    """DRAM bytes per level launch from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_expand_plain_at_scale.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_level_launch:"):
+                return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
 
 
 def dist_info():
@@ -126,7 +162,8 @@ def load_workload(name):
 
 
 def root_ranges(V, world):
-    return [(V * r // world, V * (r + 1) // world) for r in range(world)]
+    from forkmatch_gb300.shard import root_ranges as _rr
+    return _rr(V, world)
 
 
 # ------------------------------------------------------------------ reference arm
@@ -317,7 +354,8 @@ def run_ours(args, rank, world, local):
             "embeddings_per_step": total / args.steps,
             "bitexact_counts": bitexact, "rows_valid_sample": rows_ok,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": None,
+                         "frac": (achieved / peak) if achieved else None, "traffic": profiled_traffic(),
+                         "traffic_source": "profiles/k_expand_plain_at_scale.md (DRAM read+write per level launch)",
                          "kernel": "k_expand (all levels)", "peak_kind": peak_kind,
                          "algorithmic_bytes_per_step": alg_bytes, "kernel_ms_per_step": kern_ms,
                          "launches_per_step": n_launch,
@@ -328,7 +366,8 @@ def run_ours(args, rank, world, local):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": best,
                     "ms_per_step": 1000 * e2e_s / args.steps},
-            "gpu_launches": launches, "clocks": clocks,
+            # every level launch is two kernels of ours: the main pass and the heavy pass
+            "gpu_launches": 2 * launches, "clocks": clocks,
             "graph": {"build_ms": ginfo.build_ms, "device_bytes": ginfo.device_bytes, "max_list": ginfo.max_list,
                       "segments": ginfo.segments, "long_segments": ginfo.long_segments,
                       "generate_s": gen_s, "load_s": build_s}}
@@ -402,6 +441,8 @@ def cpu_baseline(wl, G, edges):
 def main():
     args = parse_args()
     rank, world, local = dist_info()
+    if args.ncu_step:
+        return run_ncu_step(args)
     if args.impl == "reference":
         return run_reference(args, rank, world)
     return run_ours(args, rank, world, local)
