@@ -2,12 +2,13 @@
 //
 // The matching driver replaces the reference's host match() (src/smsm.cu:1182-1349)
 // and its device-side fork machinery (src/smsm.cu:564-687, 949-1139: CDP child
-// launches on bank overflow, tail-launched bank frees).  Here the host walks
-// the levels depth first: it launches one expansion kernel per level, reads a
-// 64-byte control block back, and when a level's buffer filled it first drains
-// the deeper levels and then relaunches the level on the chunks that were
-// deferred.  Memory is therefore bounded by SOLN_PREALLOC (one buffer per
-// depth) and no device code waits on anything.
+// launches on bank overflow, tail-launched bank frees).  All levels of a query
+// are launched back to back, each reading its parent count from the previous
+// level's control block on the device, and the host synchronises once.  If a
+// level's buffer filled, the host then walks the levels depth first: it drains
+// the deeper levels and relaunches the level on the chunks it deferred or did
+// not claim.  Memory is bounded by SOLN_PREALLOC (one buffer per depth) and
+// no device code waits on anything.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -184,13 +185,14 @@ fm_status fm_context_create(const fm_knobs* knobs, fm_context** out) {
     char* misc = c->slab + ((k.prealloc_bytes - kMiscBytes) & ~255ull);
     // [0, 4 KiB) control blocks, [4 KiB, 48 MiB) deferred-chunk lists (two per
     // depth), [48 MiB, 64 MiB) heavy-chunk entries
-    c->ctl = (LaunchCtl*)misc;
-    c->tot = (MatchTotals*)(misc + 512);
-    c->defs = (uint32_t*)(misc + 4096);
-    c->def_cap = (uint32_t)(((48ull << 20) - 4096) / 4 / (2 * kMaxQ));
+    static_assert(kMaxQ * sizeof(LaunchCtl) <= 4096, "per-level control blocks must fit in 4 KiB");
+    c->ctl = (LaunchCtl*)misc;                 // one control block per depth
+    c->tot = (MatchTotals*)(misc + 4096);
+    c->defs = (uint32_t*)(misc + 8192);
+    c->def_cap = (uint32_t)(((48ull << 20) - 8192) / 4 / (2 * kMaxQ));
     c->heavy = (HeavyEntry*)(misc + (48ull << 20));
     c->heavy_cap = (uint32_t)((kMiscBytes - (48ull << 20)) / sizeof(HeavyEntry));
-    FM_CUDA(cudaHostAlloc(&c->h_ctl, sizeof(LaunchCtl), cudaHostAllocDefault));
+    FM_CUDA(cudaHostAlloc(&c->h_ctl, kMaxQ * sizeof(LaunchCtl), cudaHostAllocDefault));
     FM_CUDA(cudaHostAlloc(&c->h_tot, sizeof(MatchTotals), cudaHostAllocDefault));
     FM_CUDA(cudaEventCreate(&c->ev0));
     FM_CUDA(cudaEventCreate(&c->ev1));
@@ -374,16 +376,117 @@ struct MatchRun {
     size_t prof_used = 0;
     int block = 256;
 
-    fm_status launch_level(uint32_t d, uint64_t n_parents, bool roots) {
+    int mode_of(uint32_t d) const {
+        return (d == plan->q - 1) ? (table ? kModeLastTable : kModeLastCount) : kModeMid;
+    }
+    uint32_t* def_list(uint32_t d, int which) const {
+        return ctx->defs + (size_t)(2 * d + which) * ctx->def_cap;
+    }
+    fm_status begin_timing(cudaEvent_t& e0, cudaEvent_t& e1) {
+        while (ctx->prof.size() < prof_used + 2) {
+            cudaEvent_t e;
+            FM_CUDA(cudaEventCreate(&e));
+            ctx->prof.push_back(e);
+        }
+        e0 = ctx->prof[prof_used++];
+        e1 = ctx->prof[prof_used++];
+        FM_CUDA(cudaEventRecord(e0, s));
+        return FM_OK;
+    }
+    void add_stats(uint32_t d, const LaunchCtl& c) {
+        fm_level_stats& ls = res->level[d];
+        ls.launches++;
+        res->launches++;
+        ls.parents += c.parents;
+        ls.lookups += c.lookups;
+        ls.list_words += c.list_words;
+        if (mode_of(d) == kModeMid) ls.produced += c.produced;
+    }
+
+    // Optimistic pass: every level launched back to back, level d reading its
+    // parent count from level d-1's control block on the device; one sync.
+    // Levels whose buffer filled (deferred or unclaimed chunks) are then
+    // resumed deepest first, so a level never writes into a buffer that a
+    // deeper level still has to read.
+    fm_status run(uint64_t n_roots) {
         const uint32_t q = plan->q;
-        const int mode = (d == q - 1) ? (table ? kModeLastTable : kModeLastCount) : kModeMid;
+        cudaEvent_t ev[kMaxQ][2] = {};
+        for (uint32_t d = 1; d < q; d++) {
+            const int mode = mode_of(d);
+            const bool roots = d == 1;
+            const size_t smem = expand_smem_bytes(d, nreq_depth[d], block / 32);
+            const int per_sm = expand_blocks_per_sm(mode, roots, dups, smem, block);
+            const int full = ctx->sms * per_sm;
+            ExpandParams p = base;
+            p.pin = roots ? nullptr : level[d];
+            p.pstride = level_cap;
+            p.depth = d;
+            p.def_in = def_list(d, 0);
+            p.ndef_in = 0;
+            p.fresh_base = 0;
+            p.def_out = def_list(d, 1);
+            p.def_cap = ctx->def_cap;
+            p.pout = (mode == kModeMid) ? level[d + 1] : nullptr;
+            p.ocap = level_cap;
+            p.ctl = ctx->ctl + d;
+            int grid = full;
+            if (roots) {
+                p.n_parents = n_roots;
+                p.n_items = (n_roots + 31) / 32;
+                grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((p.n_items + 7) / 8, (uint64_t)full));
+            } else {
+                p.n_parents_dev = &ctx->ctl[d - 1].produced;
+            }
+            FM_CUDA(cudaMemsetAsync(ctx->ctl + d, 0, sizeof(LaunchCtl), s));
+            if (profile) FM_TRY(begin_timing(ev[d][0], ev[d][1]));
+            FM_CUDA(launch_expand(p, mode, roots, dups, grid, full, block, smem, s));
+            if (profile) FM_CUDA(cudaEventRecord(ev[d][1], s));
+        }
+        FM_CUDA(cudaMemcpyAsync(ctx->h_ctl, ctx->ctl, q * sizeof(LaunchCtl), cudaMemcpyDeviceToHost, s));
+        FM_CUDA(cudaStreamSynchronize(s));
+        uint64_t n_parents[kMaxQ] = {};
+        for (uint32_t d = 1; d < q; d++) {
+            const LaunchCtl& c = ctx->h_ctl[d];
+            n_parents[d] = d == 1 ? n_roots : ctx->h_ctl[d - 1].produced;
+            add_stats(d, c);
+            if (profile) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, ev[d][0], ev[d][1]);
+                res->level[d].kernel_ms += ms;
+            }
+            if (c.error) {
+                set_error("deferred-chunk list overflow");
+                return FM_ERR_DEVICE;
+            }
+        }
+        LaunchCtl snap[kMaxQ];
+        std::memcpy(snap, ctx->h_ctl, q * sizeof(LaunchCtl));
+        for (uint32_t d = q - 1; d >= 1; d--) {
+            if (mode_of(d) != kModeMid) continue;   // the last level never defers
+            const LaunchCtl& c = snap[d];
+            const uint64_t items = (n_parents[d] + 31) / 32;
+            const uint64_t claimed = std::min<uint64_t>(c.claim, items);
+            if (c.ndef == 0 && claimed == items) continue;
+            // every chunk claimed in the optimistic pass was fresh and was either
+            // processed or deferred (its id is in the pass's def_out list)
+            fm_status st = drain_level(d, n_parents[d], d == 1, c.ndef, claimed, def_list(d, 1), def_list(d, 0));
+            if (st != FM_OK) return st;
+        }
+        return FM_OK;
+    }
+
+    // Host-driven depth-first loop for one level (used when a level's buffer
+    // filled): relaunch on deferred + unclaimed chunks, draining deeper levels
+    // after every launch.  `fresh` counts fresh chunks already processed or
+    // deferred; `def_a` holds `ndef_in` deferred chunk ids.
+    fm_status drain_level(uint32_t d, uint64_t n_parents, bool roots, uint32_t ndef_in, uint64_t fresh,
+                          uint32_t* def_a, uint32_t* def_b) {
+        const uint32_t q = plan->q;
+        const int mode = mode_of(d);
         const uint64_t n_chunks = (n_parents + 31) / 32;
-        uint32_t* def_a = ctx->defs + (size_t)(2 * d) * ctx->def_cap;
-        uint32_t* def_b = def_a + ctx->def_cap;
-        uint32_t ndef_in = 0;
-        uint64_t fresh = 0;
         const size_t smem = expand_smem_bytes(d, nreq_depth[d], block / 32);
         const int per_sm = expand_blocks_per_sm(mode, roots, dups, smem, block);
+        (void)q;
         while (true) {
             const uint64_t items = ndef_in + (n_chunks - fresh);
             if (items == 0) break;
@@ -400,37 +503,24 @@ struct MatchRun {
             p.def_cap = ctx->def_cap;
             p.pout = (mode == kModeMid) ? level[d + 1] : nullptr;
             p.ocap = level_cap;
+            p.ctl = ctx->ctl + d;
             uint64_t want = (items + (block / 32) - 1) / (block / 32);
             int grid = (int)std::min<uint64_t>(want, (uint64_t)ctx->sms * per_sm);
             if (grid < 1) grid = 1;
-            FM_CUDA(cudaMemsetAsync(ctx->ctl, 0, sizeof(LaunchCtl), s));
+            FM_CUDA(cudaMemsetAsync(ctx->ctl + d, 0, sizeof(LaunchCtl), s));
             cudaEvent_t e0 = nullptr, e1 = nullptr;
-            if (profile) {
-                while (ctx->prof.size() < prof_used + 2) {
-                    cudaEvent_t e;
-                    FM_CUDA(cudaEventCreate(&e));
-                    ctx->prof.push_back(e);
-                }
-                e0 = ctx->prof[prof_used];
-                e1 = ctx->prof[prof_used + 1];
-                FM_CUDA(cudaEventRecord(e0, s));
-            }
+            if (profile) FM_TRY(begin_timing(e0, e1));
             FM_CUDA(launch_expand(p, mode, roots, dups, grid, ctx->sms * per_sm, block, smem, s));
             if (profile) FM_CUDA(cudaEventRecord(e1, s));
-            FM_CUDA(cudaMemcpyAsync(ctx->h_ctl, ctx->ctl, sizeof(LaunchCtl), cudaMemcpyDeviceToHost, s));
+            FM_CUDA(cudaMemcpyAsync(ctx->h_ctl + d, ctx->ctl + d, sizeof(LaunchCtl), cudaMemcpyDeviceToHost, s));
             FM_CUDA(cudaStreamSynchronize(s));
-            const LaunchCtl c = *ctx->h_ctl;
-            fm_level_stats& ls = res->level[d];
+            const LaunchCtl c = ctx->h_ctl[d];
             if (profile) {
                 float ms = 0;
                 cudaEventElapsedTime(&ms, e0, e1);
-                ls.kernel_ms += ms;
+                res->level[d].kernel_ms += ms;
             }
-            ls.launches++;
-            res->launches++;
-            ls.parents += c.parents;
-            ls.lookups += c.lookups;
-            ls.list_words += c.list_words;
+            add_stats(d, c);
             if (c.error) {
                 set_error("deferred-chunk list overflow");
                 return FM_ERR_DEVICE;
@@ -449,14 +539,13 @@ struct MatchRun {
                 ndef_out += carry;
             }
             if (mode == kModeMid) {
-                ls.produced += c.produced;
                 const uint64_t done_chunks = claimed - c.ndef;
                 if (done_chunks == 0 && c.produced == 0 && ndef_out == items) {
                     set_error("one 32-parent chunk needs more rows than a level buffer holds; raise SOLN_PREALLOC");
                     return FM_ERR_POOL;
                 }
                 if (c.produced) {
-                    fm_status st = launch_level(d + 1, c.produced, false);
+                    fm_status st = drain_level(d + 1, c.produced, false, 0, 0, def_list(d + 1, 0), def_list(d + 1, 1));
                     if (st != FM_OK) return st;
                 }
             }
@@ -610,7 +699,7 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         b.tot = ctx->tot;
         b.heavy = ctx->heavy;
         b.heavy_cap = ctx->heavy_cap;
-        fm_status st = run.launch_level(1, re - rb, true);
+        fm_status st = run.run(re - rb);
         if (st != FM_OK) return st;
     }
     FM_CUDA(cudaEventRecord(ctx->ev1, s));

@@ -25,6 +25,12 @@ fm_status cuda_fail(cudaError_t e, const char* what);
         if (_e != cudaSuccess) return ::fm::cuda_fail(_e, #call); \
     } while (0)
 
+#define FM_TRY(call)                       \
+    do {                                   \
+        fm_status _s = (call);             \
+        if (_s != FM_OK) return _s;        \
+    } while (0)
+
 // ----------------------------------------------------------------- data graph
 // Segment record of one (label, vertex) list, one 16-byte load per lookup:
 //   len <= 3 : {len, n0, n1, n2}      neighbours inline, unused slots 0xffffffff
@@ -130,6 +136,10 @@ struct ExpandParams {
     const uint32_t* pin;            // SoA: column c at pin + c*pstride (null for roots)
     uint64_t pstride;
     uint64_t n_parents;
+    // when set, n_parents is read on the device from here (the previous level's
+    // `produced`) and the launch covers fresh chunks only: levels can then be
+    // launched back to back without the host reading anything in between
+    const unsigned long long* n_parents_dev;
     uint32_t root_begin;            // roots: parent p is vertex root_begin + p
     uint32_t depth;                 // parent rows have `depth` entries; new vertex goes to column depth
     // work items
@@ -149,12 +159,7 @@ struct ExpandParams {
     MatchTotals* tot;
     HeavyEntry* heavy;
     uint32_t heavy_cap;             // entries; chunks are published only while room remains
-    uint32_t max_warps;             // warps of the launch (bounds concurrent publishers)
-    // launch tuning, set by launch_expand
-    uint32_t claim_batch;           // chunks claimed per atomic
-    uint32_t credit_block;          // output rows reserved per budget atomic
-    uint32_t heavy_thresh;          // candidate slots above which a chunk is split
-    uint32_t heavy_piece;           // slots per piece of a split chunk
+    uint32_t max_warps;             // warps of the heavy pass (bounds concurrent publishers)
 };
 
 // Launch one level expansion: the main pass, then the heavy-chunk pass

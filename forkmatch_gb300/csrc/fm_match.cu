@@ -87,6 +87,41 @@ __device__ __forceinline__ uint32_t seg_rank(const uint4& s, uint32_t t, uint32_
     return t - lower_bound_g(a, t, x);
 }
 
+// Launch tuning, computed on the device from the level's actual size, so a
+// launch whose parent count is only known on the device is tuned the same way.
+// Both passes derive the split parameters from the same inputs.
+struct Tune {
+    unsigned long long n_parents, n_items;
+    uint32_t claim_batch;    // chunks claimed per atomic (keeps ~2 claims per warp on big levels)
+    uint32_t credit_block;   // output rows reserved per budget atomic; idle credit stays under 1/4 of the level
+    uint32_t heavy_thresh;   // candidate slots above which a chunk is split: finer when chunks are few
+    uint32_t heavy_piece;    // slots per piece of a split chunk
+};
+
+__device__ __forceinline__ Tune make_tune(const ExpandParams& P, bool main_pass) {
+    Tune t;
+    if (P.n_parents_dev) {
+        t.n_parents = *(const volatile unsigned long long*)P.n_parents_dev;
+        t.n_items = (t.n_parents + 31) / 32;
+    } else {
+        t.n_parents = P.n_parents;
+        t.n_items = P.n_items;
+    }
+    const unsigned long long all_warps = P.max_warps ? P.max_warps : 1;
+    if (main_pass) {
+        const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
+        const unsigned long long per_warp = t.n_items / warps + 1;
+        t.claim_batch = (uint32_t)(per_warp / 2 < 1 ? 1 : (per_warp / 2 > 8 ? 8 : per_warp / 2));
+    } else {
+        t.claim_batch = 1;
+    }
+    const unsigned long long cb = P.ocap / (4 * all_warps);
+    t.credit_block = (uint32_t)(cb < 1024 ? cb : 1024);
+    t.heavy_thresh = t.n_items >= 4 * all_warps ? 4096u : (t.n_items >= all_warps ? 1024u : 256u);
+    t.heavy_piece = t.heavy_thresh / 2;
+    return t;
+}
+
 __device__ __forceinline__ uint32_t item_chunk(const ExpandParams& P, unsigned long long item) {
     return item < P.ndef_in ? P.def_in[item] : (uint32_t)(P.fresh_base + (item - P.ndef_in));
 }
@@ -213,10 +248,10 @@ __device__ __forceinline__ void flush_stage(const ExpandParams& P, const WarpMem
 // driver lengths.  Returns the chunk's candidate slots (warp-uniform).
 template <bool ROOTS>
 __device__ __forceinline__ uint32_t load_chunk(const ExpandParams& P, const WarpMem& m, uint32_t chunk, uint32_t lane,
-                                               uint32_t d, uint32_t k, uint32_t rb, bool& valid,
-                                               unsigned long long& words) {
+                                               uint32_t d, uint32_t k, uint32_t rb, unsigned long long n_parents,
+                                               bool& valid, unsigned long long& words) {
     const uint64_t p = (uint64_t)chunk * 32 + lane;
-    valid = p < P.n_parents;
+    valid = p < n_parents;
     if (ROOTS) {
         m.rows_s[lane] = P.root_begin + (uint32_t)p;
     } else {
@@ -321,6 +356,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
     const uint32_t k = P.plan.nreq[d];
     const uint32_t rb = P.plan.req_begin[d];
     const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k);
+    const Tune T = make_tune(P, true);
 
     unsigned long long n_count = 0, n_lookups = 0, n_words = 0, n_parents = 0;
     unsigned long long credit = 0;   // level budget held by this warp (lane 0)
@@ -328,11 +364,11 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
     bool done = false;
     while (!done) {
         unsigned long long first = 0;
-        if (lane == 0) first = atomicAdd(&P.ctl->claim, (unsigned long long)P.claim_batch);
+        if (lane == 0) first = atomicAdd(&P.ctl->claim, (unsigned long long)T.claim_batch);
         first = __shfl_sync(kFull, first, 0);
-        if (first >= P.n_items) break;
+        if (first >= T.n_items) break;
         const unsigned long long last =
-            first + P.claim_batch < P.n_items ? first + P.claim_batch : (unsigned long long)P.n_items;
+            first + T.claim_batch < T.n_items ? first + T.claim_batch : T.n_items;
         for (unsigned long long item = first; item < last; item++) {
             const uint32_t chunk = item_chunk(P, item);
             if (MODE == kModeMid) {
@@ -349,12 +385,12 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
             }
             bool valid;
             unsigned long long w;
-            const uint32_t total = load_chunk<ROOTS>(P, m, chunk, lane, d, k, rb, valid, w);
+            const uint32_t total = load_chunk<ROOTS>(P, m, chunk, lane, d, k, rb, T.n_parents, valid, w);
             if (MODE == kModeMid && total) {
                 int ok = 1;
                 if (lane == 0) {
                     if (total > credit) {
-                        const unsigned long long need = max((unsigned long long)total, (unsigned long long)P.credit_block);
+                        const unsigned long long need = max((unsigned long long)total, (unsigned long long)T.credit_block);
                         const unsigned long long old = atomicAdd(&P.ctl->budget, need);
                         if (old + need > P.ocap) {
                             ok = 0;
@@ -377,12 +413,12 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
                 n_words += w;
                 n_parents += 1;
             }
-            if (total > P.heavy_thresh) {
+            if (total > T.heavy_thresh) {
                 // Publish: one packed atomic reserves the entry index and its
                 // piece range, so entries are ordered by first piece.  The room
                 // check is conservative: at most max_warps publishers are past it.
                 int pub = 0;
-                const uint32_t np = (total + P.heavy_piece - 1) / P.heavy_piece;
+                const uint32_t np = (total + T.heavy_piece - 1) / T.heavy_piece;
                 if (lane == 0 && np <= kHeavyMaxPieces) {
                     const unsigned long long h = *(volatile unsigned long long*)&P.ctl->heavy;
                     if ((uint32_t)(h >> 32) + P.max_warps < P.heavy_cap && (uint32_t)h < (1u << 31)) {
@@ -437,6 +473,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand_heavy(const __grid_co
     const uint32_t k = P.plan.nreq[d];
     const uint32_t rb = P.plan.req_begin[d];
     const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k);
+    const Tune T = make_tune(P, false);
     unsigned long long n_count = 0;
     uint32_t nst = 0;
     for (;;) {
@@ -451,11 +488,11 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand_heavy(const __grid_co
             else hi = mid;
         }
         const HeavyEntry e = P.heavy[lo];
-        const uint32_t begin = ((uint32_t)gp - e.piece0) * P.heavy_piece;
-        const uint32_t end = min(begin + P.heavy_piece, e.total);
+        const uint32_t begin = ((uint32_t)gp - e.piece0) * T.heavy_piece;
+        const uint32_t end = min(begin + T.heavy_piece, e.total);
         bool valid;
         unsigned long long w;
-        load_chunk<ROOTS>(P, m, e.chunk, lane, d, k, rb, valid, w);
+        load_chunk<ROOTS>(P, m, e.chunk, lane, d, k, rb, T.n_parents, valid, w);
         process_slots<MODE, ROOTS, DUPS>(P, m, e.chunk, begin, end, lane, d, k, col_depth_s, nst, n_count);
     }
     if (MODE != kModeLastCount && nst) flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s);
@@ -503,18 +540,9 @@ cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups
     void* fh = pick(mode, roots, dups, true);
     if (!f || !fh) return cudaErrorInvalidValue;
     ExpandParams q = p;
-    const uint32_t warps = (uint32_t)(block / 32);
-    q.max_warps = (uint32_t)heavy_grid * warps;
-    // Claims: several chunks per atomic on large levels (keeps ~16 claims per warp).
-    const uint64_t per_warp_items = q.n_items / ((uint64_t)grid * warps) + 1;
-    q.claim_batch = (uint32_t)std::min<uint64_t>(8, std::max<uint64_t>(1, per_warp_items / 16));
-    // Output budget is reserved in blocks small enough that the budget idle in
-    // all warps stays under a quarter of the level.
-    q.credit_block = (uint32_t)std::min<uint64_t>(1024, q.ocap / (4ull * std::max<uint32_t>(1, q.max_warps)));
-    // Split threshold: the fewer chunks a level has per warp, the finer the pieces.
-    const uint64_t all_warps = (uint64_t)heavy_grid * warps;
-    q.heavy_thresh = q.n_items >= 4 * all_warps ? 4096u : (q.n_items >= all_warps ? 1024u : 256u);
-    q.heavy_piece = q.heavy_thresh / 2;
+    // both passes tune themselves on the device (make_tune) from the level size
+    // and from max_warps, the warps of the heavy pass
+    q.max_warps = (uint32_t)heavy_grid * (uint32_t)(block / 32);
     void* args[] = {(void*)&q};
     cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(block), args, smem, s);
     if (e != cudaSuccess) return e;
