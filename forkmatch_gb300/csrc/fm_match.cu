@@ -109,9 +109,12 @@ __device__ __forceinline__ Tune make_tune(const ExpandParams& P, bool main_pass)
     }
     const unsigned long long all_warps = P.max_warps ? P.max_warps : 1;
     if (main_pass) {
+        // roots cost the same per chunk, so they can be claimed in big batches;
+        // deeper chunks vary, so batches stay small there to keep warps balanced
         const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
         const unsigned long long per_warp = t.n_items / warps + 1;
-        t.claim_batch = (uint32_t)(per_warp / 2 < 1 ? 1 : (per_warp / 2 > 8 ? 8 : per_warp / 2));
+        const unsigned long long b = per_warp / (P.pin ? 16 : 2);
+        t.claim_batch = (uint32_t)(b < 1 ? 1 : (b > 8 ? 8 : b));
     } else {
         t.claim_batch = 1;
     }
