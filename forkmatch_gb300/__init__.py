@@ -34,7 +34,8 @@ EXPORTS = [
     "fm_context_stream", "fm_graph_load_file", "fm_graph_load_text", "fm_graph_from_edges", "fm_graph_get_info",
     "fm_graph_free", "fm_query_compile_file", "fm_query_compile_text", "fm_query_get_info", "fm_query_free",
     "fm_match_opts_default", "fm_match", "fm_host_alloc", "fm_host_free", "fm_version", "fm_device_count",
-    "fm_match_static",
+    "fm_match_static", "fm_batch_create", "fm_batch_run", "fm_batch_rows", "fm_batch_copy_rows", "fm_batch_tune",
+    "fm_batch_free",
 ]
 
 
@@ -80,6 +81,12 @@ class Result(ctypes.Structure):
                 ("d2h_bytes", ctypes.c_uint64), ("level", LevelStats * MAXQ)]
 
 
+class BatchStats(ctypes.Structure):
+    _fields_ = [("embeddings", ctypes.c_uint64), ("launches", ctypes.c_uint64), ("wall_ms", ctypes.c_double),
+                ("batched_queries", ctypes.c_uint32), ("single_queries", ctypes.c_uint32),
+                ("piece_shift", ctypes.c_uint32), ("grid_quarters", ctypes.c_uint32)]
+
+
 _lib = None
 
 
@@ -115,6 +122,12 @@ def lib():
         L.fm_host_alloc.restype = vp
         L.fm_host_free.argtypes = [vp]
         L.fm_match_static.argtypes = [vp, vp, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64), vp]
+        L.fm_batch_create.argtypes = [vp, vp, ctypes.POINTER(vp), u32, i32, ctypes.POINTER(vp)]
+        L.fm_batch_run.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(BatchStats)]
+        L.fm_batch_rows.argtypes = [vp, u32, ctypes.POINTER(vp), ctypes.POINTER(u64)]
+        L.fm_batch_copy_rows.argtypes = [vp, u32, vp, u64, ctypes.POINTER(u64)]
+        L.fm_batch_tune.argtypes = [vp, ctypes.POINTER(BatchStats)]
+        L.fm_batch_free.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -295,6 +308,46 @@ def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_ro
     st = lib().fm_match(ctx._h, graph._h, query._h, ctypes.byref(o), ctypes.byref(r))
     _check(st, "fm_match", allow=(FM_ERR_OUTPUT_OVERFLOW,) if allow_truncation else ())
     return r
+
+
+class Batch:
+    """Many queries against one resident graph in shared level launches
+    (fm_batch_*), replayed as a CUDA graph after the first run."""
+
+    def __init__(self, ctx, graph, queries, mode=MODE_COUNT):
+        self.ctx, self.graph, self.queries = ctx, graph, list(queries)
+        arr = (ctypes.c_void_p * len(self.queries))(*[q._h for q in self.queries])
+        h = ctypes.c_void_p()
+        _check(lib().fm_batch_create(ctx._h, graph._h, arr, len(self.queries), mode, ctypes.byref(h)),
+               "fm_batch_create")
+        self._h = h
+
+    def run(self, allow_truncation=False):
+        counts = (ctypes.c_uint64 * max(1, len(self.queries)))()
+        st = BatchStats()
+        s = lib().fm_batch_run(self._h, counts, ctypes.byref(st))
+        _check(s, "fm_batch_run", allow=(FM_ERR_OUTPUT_OVERFLOW,) if allow_truncation else ())
+        return [int(counts[i]) for i in range(len(self.queries))], st
+
+    def rows(self, i, max_rows):
+        q = self.queries[i].q
+        buf = np.zeros(max(1, max_rows) * q, dtype=np.uint32)
+        n = ctypes.c_uint64()
+        _check(lib().fm_batch_copy_rows(self._h, i, buf.ctypes.data, max_rows, ctypes.byref(n)), "fm_batch_copy_rows")
+        return buf[: n.value * q].reshape(-1, q)
+
+    def tune(self):
+        st = BatchStats()
+        _check(lib().fm_batch_tune(self._h, ctypes.byref(st)), "fm_batch_tune")
+        return st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fm_batch_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 def match_static(graph, query, rows_device_ptr=None, rows_cap=0, stream=None, allow_truncation=False):

@@ -1,0 +1,907 @@
+// fm_batch.cu -- batched matching: many queries against one resident graph in
+// shared level launches, captured once as a CUDA graph and replayed.
+//
+// The reference matches one query per program run (src/smsm.cu:1182-1349).
+// Here a batch of queries advances level-synchronously: the level-d launch
+// extends the partial matches of every query that is still open at depth d.
+// Rows carry their query id in an extra column, every lane reads its own
+// query's plan (requirements, table layout), and a survivor whose query ends
+// at this depth goes straight to that query's count or table region, grouped
+// per query with __match_any_sync (one atomic per query per warp round);
+// survivors of longer queries are staged and flushed into the next level like
+// in fm_match.cu.  So a batch needs max(q) - 1 level launches instead of
+// sum(q - 1), and one host synchronisation.  Graphs with duplicate e-lines
+// and single-vertex queries are matched one by one through fm_match.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "fm_device.cuh"
+
+namespace fm {
+
+struct BatchPlan {                    // per query, in device memory
+    uint32_t q;
+    uint32_t nreq[kMaxQ];
+    uint32_t req_begin[kMaxQ];
+    uint8_t req_anc[kMaxReqTotal];
+    uint8_t req_label[kMaxReqTotal];
+    uint8_t col_depth[kMaxQ];         // depth whose vertex fills table column c
+    uint64_t table_base;              // u32 offset of the query's table region
+    uint64_t table_cap;               // rows
+};
+
+struct BatchParams {
+    const BatchPlan* plans;
+    uint32_t nq;
+    const uint4* seg;
+    const uint32_t* nbr;
+    uint32_t V;
+    // parents: columns 0..d-1, query id in column d (null at depth 1: roots)
+    const uint32_t* pin;
+    uint64_t pstride;
+    uint64_t n_parents;                       // roots: nq * chunks_per_query * 32
+    const unsigned long long* n_parents_dev;  // set: read on the device (fresh chunks only)
+    uint32_t chunks_per_query;                // roots: ceil(V / 32)
+    uint32_t depth;
+    uint32_t kmax;                            // segment records per parent reserved in shared memory
+    // work items
+    const uint32_t* def_in;
+    uint32_t ndef_in;
+    uint64_t fresh_base;
+    uint64_t n_items;
+    uint32_t* def_out;
+    uint32_t def_cap;
+    // outputs: next level (columns 0..d, query id in column d+1), per-query results
+    uint32_t* pout;
+    uint64_t ocap;
+    uint32_t* table;
+    unsigned long long* qpos;                 // per query: rows reserved (table) or count
+    uint32_t table_mode;
+    LaunchCtl* ctl;
+    HeavyEntry* heavy;
+    uint32_t heavy_cap;
+    uint32_t max_warps;
+    uint32_t piece_shift;                     // autotuned: heavy threshold and piece size scale
+};
+
+namespace {
+
+using dev::kFull;
+using dev::ldg4;
+using dev::seg_at;
+using dev::seg_has;
+using dev::slot_locate;
+
+constexpr int kBWarps = 8;
+constexpr uint32_t kBStage = 256;
+constexpr uint32_t kHeavyMaxPieces = 65536;
+
+struct BTune {
+    unsigned long long n_parents, n_items;
+    uint32_t credit_block, heavy_thresh, heavy_piece;
+};
+
+__device__ __forceinline__ BTune make_btune(const BatchParams& P) {
+    BTune t;
+    if (P.n_parents_dev) {
+        t.n_parents = *(const volatile unsigned long long*)P.n_parents_dev;
+        t.n_items = (t.n_parents + 31) / 32;
+    } else {
+        t.n_parents = P.n_parents;
+        t.n_items = P.n_items;
+    }
+    const unsigned long long all_warps = P.max_warps ? P.max_warps : 1;
+    const unsigned long long cb = P.ocap / (4 * all_warps);
+    t.credit_block = (uint32_t)(cb < 1024 ? cb : 1024);
+    const uint32_t base = t.n_items >= 4 * all_warps ? 2048u : (t.n_items >= all_warps ? 512u : 128u);
+    t.heavy_piece = base << P.piece_shift;
+    t.heavy_thresh = 2 * t.heavy_piece;
+    return t;
+}
+
+// Per-warp shared memory: rows, records, drivers, per-parent query data, stage.
+struct BMem {
+    uint32_t* rows_s;   // [d][32]
+    uint4* segs_s;      // [kmax][32]
+    uint32_t* excl_s;   // [32]
+    uint32_t* drv_s;    // [32]
+    uint32_t* k_s;      // [32] requirements of the parent's query at this depth
+    uint32_t* qid_s;    // [32]
+    uint32_t* pidx_s;   // [32] parent index in the level (root vertex at depth 1)
+    uint32_t* fin_s;    // [32] 1 when the parent's query ends at depth d+1
+    uint32_t* stp;      // [kBStage] staged parent index
+    uint32_t* stx;      // [kBStage] staged vertex
+    uint32_t* stq;      // [kBStage] staged query id
+};
+
+__host__ __device__ constexpr uint32_t bper_warp_bytes(uint32_t d, uint32_t kmax) {
+    return 128 * d + 512 * kmax + 6 * 128 + 12 * kBStage;
+}
+
+__device__ __forceinline__ BMem bmem(unsigned char* smem, uint32_t warp, uint32_t d, uint32_t kmax) {
+    unsigned char* w = smem + warp * bper_warp_bytes(d, kmax);
+    BMem m;
+    m.rows_s = (uint32_t*)w;
+    m.segs_s = (uint4*)(w + 128 * d);
+    uint32_t* s = (uint32_t*)(w + 128 * d + 512 * kmax);
+    m.excl_s = s;
+    m.drv_s = s + 32;
+    m.k_s = s + 64;
+    m.qid_s = s + 96;
+    m.pidx_s = s + 128;
+    m.fin_s = s + 160;
+    m.stp = s + 192;
+    m.stx = m.stp + kBStage;
+    m.stq = m.stx + kBStage;
+    return m;
+}
+
+template <bool ROOTS>
+__device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem& m, uint32_t chunk, uint32_t lane,
+                                                uint32_t d, unsigned long long n_parents, bool& valid,
+                                                uint32_t& k_out, unsigned long long& words) {
+    uint32_t qid, pidx;
+    if (ROOTS) {
+        qid = chunk / P.chunks_per_query;
+        pidx = (chunk - qid * P.chunks_per_query) * 32 + lane;   // the root vertex
+        valid = qid < P.nq && pidx < P.V;
+        m.rows_s[lane] = pidx;
+    } else {
+        const uint64_t p = (uint64_t)chunk * 32 + lane;
+        valid = p < n_parents;
+        pidx = (uint32_t)p;
+        qid = valid ? __ldg(P.pin + (uint64_t)d * P.pstride + p) : 0u;
+        for (uint32_t c = 0; c < d; c++) m.rows_s[c * 32 + lane] = valid ? __ldg(P.pin + c * P.pstride + p) : 0u;
+    }
+    uint32_t n = 0, drv = 0, k = 0, fin = 0;
+    words = 0;
+    if (valid) {
+        const BatchPlan& pl = P.plans[qid];
+        k = pl.nreq[d];
+        fin = (pl.q == d + 1) ? 1u : 0u;
+        const uint32_t rb = pl.req_begin[d];
+        uint32_t best = 0xffffffffu;
+        for (uint32_t i = 0; i < k; i++) {
+            const uint32_t anc = pl.req_anc[rb + i];
+            const uint32_t lab = pl.req_label[rb + i];
+            const uint32_t v = m.rows_s[anc * 32 + lane];
+            const uint4 sg = ldg4(P.seg + (uint64_t)lab * P.V + v);
+            m.segs_s[i * 32 + lane] = sg;
+            words += sg.x;
+            if (sg.x < best) {
+                best = sg.x;
+                drv = i;
+            }
+        }
+        n = best;
+    }
+    k_out = k;
+    uint32_t incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if ((int)lane >= o) incl += t;
+    }
+    m.excl_s[lane] = incl - n;
+    m.drv_s[lane] = drv;
+    m.k_s[lane] = k;
+    m.qid_s[lane] = qid;
+    m.pidx_s[lane] = pidx;
+    m.fin_s[lane] = fin;
+    __syncwarp();
+    return __shfl_sync(kFull, incl, 31);
+}
+
+template <bool ROOTS>
+__device__ __forceinline__ void bflush(const BatchParams& P, const BMem& m, uint32_t nst, uint32_t lane, uint32_t d) {
+    unsigned long long pos0 = 0;
+    if (lane == 0) pos0 = atomicAdd(&P.ctl->produced, (unsigned long long)nst);
+    pos0 = __shfl_sync(kFull, pos0, 0);
+    for (uint32_t c = 0; c < d; c++) {
+        uint32_t* col = P.pout + c * P.ocap + pos0;
+        for (uint32_t i = lane; i < nst; i += 32)
+            col[i] = ROOTS ? m.stp[i] : __ldg(P.pin + c * P.pstride + m.stp[i]);
+    }
+    uint32_t* colx = P.pout + d * P.ocap + pos0;
+    uint32_t* colq = P.pout + (d + 1) * P.ocap + pos0;
+    for (uint32_t i = lane; i < nst; i += 32) {
+        colx[i] = m.stx[i];
+        colq[i] = m.stq[i];
+    }
+}
+
+// A survivor whose query ends at depth d+1: count it, or write its row into
+// the query's table region.  Lanes of the same query share one atomic.
+__device__ __forceinline__ void bfinal(const BatchParams& P, const BMem& m, bool okf, uint32_t j, uint32_t x,
+                                       uint32_t lane, uint32_t d) {
+    const unsigned fmask = __ballot_sync(kFull, okf);
+    if (!fmask || !okf) return;
+    const uint32_t qid = m.qid_s[j];
+    const unsigned grp = __match_any_sync(fmask, qid);
+    const int leader = __ffs(grp) - 1;
+    unsigned long long base = 0;
+    if ((int)lane == leader) base = atomicAdd(&P.qpos[qid], (unsigned long long)__popc(grp));
+    base = __shfl_sync(grp, base, leader);
+    if (!P.table_mode) return;
+    const BatchPlan& pl = P.plans[qid];
+    const unsigned long long pos = base + __popc(grp & ((1u << lane) - 1u));
+    if (pos >= pl.table_cap) return;
+    uint32_t* o = P.table + pl.table_base + pos * pl.q;
+    for (uint32_t c = 0; c < pl.q; c++) {
+        const uint32_t dep = pl.col_depth[c];
+        o[c] = dep < d ? m.rows_s[dep * 32 + j] : x;
+    }
+}
+
+template <bool ROOTS>
+__device__ __forceinline__ void bprocess(const BatchParams& P, const BMem& m, uint32_t begin, uint32_t end,
+                                         uint32_t lane, uint32_t d, uint32_t& nst) {
+    for (uint32_t base = begin; base < end; base += 32) {
+        const uint32_t s = base + lane;
+        bool ok = false;
+        uint32_t j = 0, x = 0;
+        if (s < end) {
+            uint32_t t;
+            slot_locate(s, m.excl_s, j, t);
+            const uint32_t dj = m.drv_s[j];
+            const uint4 ds = m.segs_s[dj * 32 + j];
+            x = seg_at(ds, t, P.nbr);
+            ok = true;
+            for (uint32_t c = 0; c < d && ok; c++) ok = m.rows_s[c * 32 + j] != x;
+            const uint32_t k = m.k_s[j];
+            for (uint32_t i = 0; i < k && ok; i++) {
+                if (i == dj) continue;
+                ok = seg_has(m.segs_s[i * 32 + j], x, 1, P.nbr);
+            }
+        }
+        const bool fin = ok && m.fin_s[j];
+        bfinal(P, m, fin, j, x, lane, d);
+        const bool stage = ok && !fin;
+        const unsigned b = __ballot_sync(kFull, stage);
+        if (stage) {
+            const uint32_t q0 = nst + __popc(b & ((1u << lane) - 1u));
+            m.stp[q0] = m.pidx_s[j];
+            m.stx[q0] = x;
+            m.stq[q0] = m.qid_s[j];
+        }
+        nst += __popc(b);
+        if (nst > kBStage - 32) {
+            __syncwarp();
+            bflush<ROOTS>(P, m, nst, lane, d);
+            nst = 0;
+        }
+        __syncwarp();
+    }
+}
+
+__device__ __forceinline__ uint32_t bitem_chunk(const BatchParams& P, unsigned long long item) {
+    return item < P.ndef_in ? P.def_in[item] : (uint32_t)(P.fresh_base + (item - P.ndef_in));
+}
+
+__device__ __forceinline__ void bdefer(const BatchParams& P, uint32_t chunk) {
+    const unsigned idx = atomicAdd(&P.ctl->ndef, 1u);
+    if (idx < P.def_cap) P.def_out[idx] = chunk;
+    else atomicOr(&P.ctl->error, 1u);
+}
+
+template <bool ROOTS>
+__global__ void __launch_bounds__(kBWarps * 32, 4) k_bexpand(const __grid_constant__ BatchParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t d = P.depth;
+    const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax);
+    const BTune T = make_btune(P);
+    unsigned long long n_lookups = 0, n_words = 0, n_parents = 0, credit = 0;
+    uint32_t nst = 0;
+    for (;;) {
+        unsigned long long item = 0;
+        if (lane == 0) item = atomicAdd(&P.ctl->claim, 1ull);
+        item = __shfl_sync(kFull, item, 0);
+        if (item >= T.n_items) break;
+        const uint32_t chunk = bitem_chunk(P, item);
+        int stop = 0;
+        if (lane == 0) stop = *(volatile unsigned int*)&P.ctl->stop ? 1 : 0;
+        stop = __shfl_sync(kFull, stop, 0);
+        if (stop) {
+            if (lane == 0) bdefer(P, chunk);
+            break;
+        }
+        bool valid;
+        uint32_t k;
+        unsigned long long w;
+        const uint32_t total = bload_chunk<ROOTS>(P, m, chunk, lane, d, T.n_parents, valid, k, w);
+        // only survivors of queries that go on use the next level's buffer;
+        // the upper bound of the whole chunk is reserved (over-reserving is safe)
+        if (total && P.pout) {
+            int ok = 1;
+            if (lane == 0 && total > credit) {
+                const unsigned long long need = max((unsigned long long)total, (unsigned long long)T.credit_block);
+                const unsigned long long old = atomicAdd(&P.ctl->budget, need);
+                if (old + need > P.ocap) {
+                    ok = 0;
+                    atomicExch(&P.ctl->stop, 1u);
+                    bdefer(P, chunk);
+                } else {
+                    credit += need;
+                }
+            }
+            if (lane == 0 && ok) credit -= total;
+            ok = __shfl_sync(kFull, ok, 0);
+            if (!ok) break;
+        }
+        if (valid) {
+            n_lookups += k;
+            n_words += w;
+            n_parents += 1;
+        }
+        if (total > T.heavy_thresh) {
+            int pub = 0;
+            const uint32_t np = (total + T.heavy_piece - 1) / T.heavy_piece;
+            if (lane == 0 && np <= kHeavyMaxPieces) {
+                const unsigned long long h = *(volatile unsigned long long*)&P.ctl->heavy;
+                if ((uint32_t)(h >> 32) + P.max_warps < P.heavy_cap && (uint32_t)h < (1u << 31)) {
+                    const unsigned long long old = atomicAdd(&P.ctl->heavy, (1ull << 32) | np);
+                    HeavyEntry e;
+                    e.chunk = chunk;
+                    e.total = total;
+                    e.piece0 = (uint32_t)old;
+                    e.pieces = np;
+                    P.heavy[(uint32_t)(old >> 32)] = e;
+                    pub = 1;
+                }
+            }
+            pub = __shfl_sync(kFull, pub, 0);
+            if (pub) continue;
+        }
+        bprocess<ROOTS>(P, m, 0, total, lane, d, nst);
+        // the stage refers to this chunk's query ids only through stq, and to
+        // its parents through pidx: it can outlive the chunk
+    }
+    if (nst) bflush<ROOTS>(P, m, nst, lane, d);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        n_lookups += __shfl_down_sync(kFull, n_lookups, o);
+        n_words += __shfl_down_sync(kFull, n_words, o);
+        n_parents += __shfl_down_sync(kFull, n_parents, o);
+    }
+    if (lane == 0 && n_parents) {
+        atomicAdd(&P.ctl->parents, n_parents);
+        atomicAdd(&P.ctl->lookups, n_lookups);
+        atomicAdd(&P.ctl->list_words, n_words);
+    }
+}
+
+template <bool ROOTS>
+__global__ void __launch_bounds__(kBWarps * 32, 4) k_bexpand_heavy(const __grid_constant__ BatchParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned long long h = P.ctl->heavy;
+    const uint32_t nent = (uint32_t)(h >> 32);
+    const uint32_t npieces = (uint32_t)h;
+    if (nent == 0) return;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t d = P.depth;
+    const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax);
+    const BTune T = make_btune(P);
+    uint32_t nst = 0;
+    for (;;) {
+        unsigned long long gp = 0;
+        if (lane == 0) gp = atomicAdd(&P.ctl->claim2, 1ull);
+        gp = __shfl_sync(kFull, gp, 0);
+        if (gp >= npieces) break;
+        uint32_t lo = 0, hi = nent;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (P.heavy[mid].piece0 <= gp) lo = mid;
+            else hi = mid;
+        }
+        const HeavyEntry e = P.heavy[lo];
+        const uint32_t begin = ((uint32_t)gp - e.piece0) * T.heavy_piece;
+        const uint32_t end = min(begin + T.heavy_piece, e.total);
+        bool valid;
+        uint32_t k;
+        unsigned long long w;
+        bload_chunk<ROOTS>(P, m, e.chunk, lane, d, T.n_parents, valid, k, w);
+        bprocess<ROOTS>(P, m, begin, end, lane, d, nst);
+    }
+    if (nst) bflush<ROOTS>(P, m, nst, lane, d);
+}
+
+cudaError_t launch_batch_level(const BatchParams& p, bool roots, int grid, int heavy_grid, size_t smem,
+                               cudaStream_t s) {
+    void* f = roots ? (void*)&k_bexpand<true> : (void*)&k_bexpand<false>;
+    void* fh = roots ? (void*)&k_bexpand_heavy<true> : (void*)&k_bexpand_heavy<false>;
+    BatchParams q = p;
+    q.max_warps = (uint32_t)heavy_grid * kBWarps;
+    void* args[] = {(void*)&q};
+    cudaError_t e = cudaLaunchKernel(f, dim3(grid), dim3(kBWarps * 32), args, smem, s);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchKernel(fh, dim3(heavy_grid), dim3(kBWarps * 32), args, smem, s);
+}
+
+int batch_blocks_per_sm(bool roots, size_t smem) {
+    void* f = roots ? (void*)&k_bexpand<true> : (void*)&k_bexpand<false>;
+    void* fh = roots ? (void*)&k_bexpand_heavy<true> : (void*)&k_bexpand_heavy<false>;
+    if (smem > 48 * 1024) {
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(fh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, kBWarps * 32, smem) != cudaSuccess || n < 1) n = 1;
+    return n;
+}
+
+}  // namespace
+}  // namespace fm
+
+// ------------------------------------------------------------------ host side
+
+using namespace fm;
+
+struct fm_batch {
+    fm_context* ctx = nullptr;
+    const fm_graph* graph = nullptr;
+    uint32_t n = 0;
+    int table = 0;
+    std::vector<const fm_query*> queries;
+    std::vector<uint32_t> batched;        // indices matched in the shared launches
+    std::vector<uint32_t> single;         // indices matched one by one (q == 1, duplicate e-lines)
+    std::vector<uint64_t> table_base, table_cap;
+    BatchPlan* d_plans = nullptr;
+    unsigned long long* d_qpos = nullptr;
+    unsigned long long* h_qpos = nullptr;
+    uint32_t maxq = 0;
+    uint32_t kmax[kMaxQ] = {};
+    uint64_t level_cap = 0;
+    uint32_t* level[kMaxQ] = {};
+    cudaGraphExec_t exec = nullptr;
+    uint32_t piece_shift = 0;
+    uint32_t sm_fraction = 4;             // quarters of the full grid used by the main pass
+    std::vector<uint64_t> counts;
+    std::vector<uint64_t> single_counts;
+    uint64_t launches = 0;
+    bool impossible_all = false;
+    std::vector<uint8_t> impossible;      // a query label absent from the graph
+};
+
+namespace {
+
+void build_plan(const Plan& pl, const DeviceGraph& g, BatchPlan& bp, bool& impossible) {
+    std::memset(&bp, 0, sizeof(bp));
+    const uint32_t q = pl.q;
+    uint32_t order[kMaxQ], nreq[kMaxQ], climb[kMaxQ][kMaxQ], rlab[kMaxQ][kMaxQ];
+    choose_order(pl, g, order);
+    if (!order_requirements(pl, order, nreq, climb, rlab)) {
+        for (uint32_t d = 0; d < q; d++) {
+            order[d] = pl.order_local[d];
+            nreq[d] = pl.nreq[d];
+            for (uint32_t i = 0; i < pl.nreq[d]; i++) {
+                climb[d][i] = pl.req_climb[d][i];
+                rlab[d][i] = pl.req_label[d][i];
+            }
+        }
+    }
+    uint32_t ref_depth[kMaxQ];
+    for (uint32_t d = 0; d < q; d++) ref_depth[pl.order_local[d]] = d;
+    bp.q = q;
+    uint32_t r = 0;
+    impossible = false;
+    for (uint32_t d = 0; d < q; d++) {
+        bp.nreq[d] = nreq[d];
+        bp.req_begin[d] = r;
+        for (uint32_t i = 0; i < nreq[d]; i++, r++) {
+            bp.req_anc[r] = (uint8_t)(d - climb[d][i]);
+            bp.req_label[r] = (uint8_t)rlab[d][i];
+            if (rlab[d][i] >= g.L) impossible = true;
+        }
+        const uint32_t col = q - 1 - ref_depth[order[d]];
+        bp.col_depth[col] = (uint8_t)d;
+    }
+}
+
+struct BatchRun {
+    fm_batch* b;
+    ContextView cv;
+    const DeviceGraph* g;
+    cudaStream_t s;
+    BatchParams base;
+    uint32_t nq;
+
+    uint32_t* def_list(uint32_t d, int which) const {
+        return cv.defs + (size_t)(2 * d + which) * cv.def_cap;
+    }
+    int gfull[kMaxQ] = {};
+    size_t smem(uint32_t d) const { return (size_t)kBWarps * bper_warp_bytes(d, b->kmax[d]); }
+    // occupancy queries and attribute changes happen here, before any capture
+    void prepare() {
+        for (uint32_t d = 1; d < b->maxq; d++) gfull[d] = cv.sms * batch_blocks_per_sm(d == 1, smem(d));
+    }
+    int full_grid(uint32_t d) const { return gfull[d]; }
+    int main_grid(uint32_t d) const { return std::max(1, full_grid(d) * (int)b->sm_fraction / 4); }
+
+    BatchParams level_params(uint32_t d) const {
+        BatchParams p = base;
+        p.depth = d;
+        p.kmax = b->kmax[d];
+        p.pin = d == 1 ? nullptr : b->level[d];
+        p.pstride = b->level_cap;
+        p.pout = (d + 1 < b->maxq) ? b->level[d + 1] : nullptr;
+        p.ocap = b->level_cap;
+        p.def_in = def_list(d, 0);
+        p.def_out = def_list(d, 1);
+        p.def_cap = cv.def_cap;
+        p.ctl = cv.ctl + d;
+        return p;
+    }
+
+    // Every level back to back; the stream work this enqueues is what the
+    // CUDA graph captures.
+    fm_status enqueue_all() {
+        FM_CUDA(cudaMemsetAsync(b->d_qpos, 0, nq * sizeof(unsigned long long), s));
+        for (uint32_t d = 1; d < b->maxq; d++) {
+            BatchParams p = level_params(d);
+            if (d == 1) {
+                p.n_parents = (uint64_t)nq * base.chunks_per_query * 32;
+                p.n_items = (uint64_t)nq * base.chunks_per_query;
+            } else {
+                p.n_parents_dev = &cv.ctl[d - 1].produced;
+            }
+            p.ndef_in = 0;
+            p.fresh_base = 0;
+            FM_CUDA(cudaMemsetAsync(cv.ctl + d, 0, sizeof(LaunchCtl), s));
+            FM_CUDA(launch_batch_level(p, d == 1, main_grid(d), full_grid(d), smem(d), s));
+        }
+        FM_CUDA(cudaMemcpyAsync(cv.h_ctl, cv.ctl, b->maxq * sizeof(LaunchCtl), cudaMemcpyDeviceToHost, s));
+        FM_CUDA(cudaMemcpyAsync(b->h_qpos, b->d_qpos, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        return FM_OK;
+    }
+
+    // Host-driven depth-first drain of level d (same protocol as fm_match).
+    fm_status drain(uint32_t d, uint64_t n_parents, uint32_t ndef_in, uint64_t fresh, uint32_t* def_a,
+                    uint32_t* def_b) {
+        const uint64_t n_chunks = d == 1 ? (uint64_t)nq * base.chunks_per_query : (n_parents + 31) / 32;
+        while (true) {
+            const uint64_t items = ndef_in + (n_chunks - fresh);
+            if (items == 0) break;
+            BatchParams p = level_params(d);
+            p.n_parents = n_parents;
+            p.n_items = items;
+            p.def_in = def_a;
+            p.ndef_in = ndef_in;
+            p.fresh_base = fresh;
+            p.def_out = def_b;
+            FM_CUDA(cudaMemsetAsync(cv.ctl + d, 0, sizeof(LaunchCtl), s));
+            const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((items + 7) / 8, (uint64_t)full_grid(d)));
+            FM_CUDA(launch_batch_level(p, d == 1, grid, full_grid(d), smem(d), s));
+            b->launches++;
+            FM_CUDA(cudaMemcpyAsync(cv.h_ctl + d, cv.ctl + d, sizeof(LaunchCtl), cudaMemcpyDeviceToHost, s));
+            FM_CUDA(cudaStreamSynchronize(s));
+            const LaunchCtl c = cv.h_ctl[d];
+            if (c.error) {
+                set_error("deferred-chunk list overflow");
+                return FM_ERR_DEVICE;
+            }
+            const uint64_t claimed = std::min<uint64_t>(c.claim, items);
+            const uint64_t fresh_claimed = claimed > ndef_in ? claimed - ndef_in : 0;
+            const uint64_t carry = ndef_in > claimed ? ndef_in - claimed : 0;
+            fresh += fresh_claimed;
+            uint64_t ndef_out = c.ndef;
+            if (ndef_out + carry > cv.def_cap) {
+                set_error("deferred-chunk list overflow");
+                return FM_ERR_DEVICE;
+            }
+            if (carry) {
+                FM_CUDA(cudaMemcpyAsync(def_b + ndef_out, def_a + claimed, carry * 4, cudaMemcpyDeviceToDevice, s));
+                ndef_out += carry;
+            }
+            if (d + 1 < b->maxq) {
+                if (claimed - c.ndef == 0 && c.produced == 0 && ndef_out == items) {
+                    set_error("one 32-parent chunk needs more rows than a level buffer holds; raise SOLN_PREALLOC");
+                    return FM_ERR_POOL;
+                }
+                if (c.produced) FM_TRY(drain(d + 1, c.produced, 0, 0, def_list(d + 1, 0), def_list(d + 1, 1)));
+            }
+            std::swap(def_a, def_b);
+            ndef_in = (uint32_t)ndef_out;
+        }
+        return FM_OK;
+    }
+
+    fm_status run(bool use_graph) {
+        prepare();
+        if (use_graph) {
+            if (!b->exec) {
+                cudaGraph_t graph = nullptr;
+                FM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                fm_status st = enqueue_all();
+                cudaError_t e = cudaStreamEndCapture(s, &graph);
+                if (st != FM_OK) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return st;
+                }
+                if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+                e = cudaGraphInstantiate(&b->exec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+            }
+            FM_CUDA(cudaGraphLaunch(b->exec, s));
+        } else {
+            FM_TRY(enqueue_all());
+        }
+        FM_CUDA(cudaStreamSynchronize(s));
+        b->launches += 2 * (b->maxq - 1);
+        LaunchCtl snap[kMaxQ];
+        std::memcpy(snap, cv.h_ctl, b->maxq * sizeof(LaunchCtl));
+        uint64_t n_parents[kMaxQ] = {};
+        for (uint32_t d = 1; d < b->maxq; d++) {
+            if (snap[d].error) {
+                set_error("deferred-chunk list overflow");
+                return FM_ERR_DEVICE;
+            }
+            n_parents[d] = d == 1 ? (uint64_t)nq * base.chunks_per_query * 32 : snap[d - 1].produced;
+        }
+        bool resumed = false;
+        for (uint32_t d = b->maxq - 1; d >= 1; d--) {
+            if (d + 1 >= b->maxq) continue;   // the last level never defers
+            const uint64_t items = d == 1 ? (uint64_t)nq * base.chunks_per_query : (n_parents[d] + 31) / 32;
+            const uint64_t claimed = std::min<uint64_t>(snap[d].claim, items);
+            if (snap[d].ndef == 0 && claimed == items) continue;
+            resumed = true;
+            FM_TRY(drain(d, n_parents[d], snap[d].ndef, claimed, def_list(d, 1), def_list(d, 0)));
+        }
+        if (resumed) {
+            FM_CUDA(cudaMemcpyAsync(b->h_qpos, b->d_qpos, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+            FM_CUDA(cudaStreamSynchronize(s));
+        }
+        return FM_OK;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+fm_status fm_batch_create(fm_context* ctx, const fm_graph* graph, const fm_query* const* queries, uint32_t n,
+                          int32_t mode, fm_batch** out) {
+    if (!ctx || !graph || !out || (n && !queries)) return FM_ERR_ARG;
+    *out = nullptr;
+    std::unique_ptr<fm_batch> b(new fm_batch());
+    b->ctx = ctx;
+    b->graph = graph;
+    b->n = n;
+    b->table = mode == FM_MODE_TABLE;
+    b->queries.assign(queries, queries + n);
+    b->counts.assign(n, 0);
+    b->impossible.assign(n, 0);
+    const DeviceGraph& g = graph->g;
+    ContextView cv = context_view(ctx);
+    if (g.device != cv.device) {
+        set_error("graph and context live on different devices");
+        return FM_ERR_ARG;
+    }
+    FM_CUDA(cudaSetDevice(cv.device));
+    std::vector<BatchPlan> plans;
+    uint64_t table_words = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        if (!queries[i]) return FM_ERR_ARG;
+        const Plan& pl = queries[i]->p;
+        if (pl.q < 2 || g.has_dups) {
+            b->single.push_back(i);
+            continue;
+        }
+        BatchPlan bp;
+        bool imp = false;
+        build_plan(pl, g, bp, imp);
+        if (imp) {
+            b->impossible[i] = 1;
+            continue;
+        }
+        b->batched.push_back(i);
+        plans.push_back(bp);
+        table_words += pl.q;
+    }
+    // table regions: the same number of rows for every batched query
+    const uint64_t rows_each = table_words ? cv.output_bytes / 4 / table_words : 0;
+    uint64_t off = 0;
+    for (auto& bp : plans) {
+        bp.table_base = off;
+        bp.table_cap = b->table ? rows_each : 0;
+        off += rows_each * bp.q;
+    }
+    for (auto& bp : plans) {
+        b->table_base.push_back(bp.table_base);
+        b->table_cap.push_back(bp.table_cap);
+        b->maxq = std::max(b->maxq, bp.q);
+    }
+    const uint32_t nq = (uint32_t)plans.size();
+    if (nq) {
+        for (uint32_t d = 1; d < b->maxq; d++) {
+            uint32_t km = 1;
+            for (auto& bp : plans)
+                if (d < bp.q) km = std::max(km, bp.nreq[d]);
+            b->kmax[d] = km;
+        }
+        uint64_t sum_cols = 0;   // level d+1 rows hold d+1 vertices and a query id
+        for (uint32_t d = 2; d < b->maxq; d++) sum_cols += d + 1;
+        uint64_t cap = sum_cols ? cv.soln_bytes / (4ull * sum_cols) : 0;
+        cap = std::min<uint64_t>(cap, 0xffffffffull - 64);
+        if (sum_cols && cap < (uint64_t)g.max_len * 32 + 32) {
+            set_error("SOLN_PREALLOC cannot hold one 32-parent chunk per level for this graph");
+            return FM_ERR_POOL;
+        }
+        b->level_cap = cap;
+        uint64_t loff = 0;
+        for (uint32_t d = 2; d < b->maxq; d++) {
+            b->level[d] = (uint32_t*)(cv.soln + loff);
+            loff += 4ull * (d + 1) * cap;
+        }
+        FM_CUDA(cudaMalloc(&b->d_plans, nq * sizeof(BatchPlan)));
+        FM_CUDA(cudaMemcpy(b->d_plans, plans.data(), nq * sizeof(BatchPlan), cudaMemcpyHostToDevice));
+        FM_CUDA(cudaMalloc(&b->d_qpos, nq * sizeof(unsigned long long)));
+        FM_CUDA(cudaHostAlloc(&b->h_qpos, nq * sizeof(unsigned long long), cudaHostAllocDefault));
+    }
+    *out = b.release();
+    return FM_OK;
+}
+
+void fm_batch_free(fm_batch* b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->d_plans) cudaFree(b->d_plans);
+    if (b->d_qpos) cudaFree(b->d_qpos);
+    if (b->h_qpos) cudaFreeHost(b->h_qpos);
+    delete b;
+}
+
+fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
+    if (!b) return FM_ERR_ARG;
+    ContextView cv = context_view(b->ctx);
+    FM_CUDA(cudaSetDevice(cv.device));
+    auto t0 = std::chrono::steady_clock::now();
+    const uint64_t launches0 = b->launches;
+    const DeviceGraph& g = b->graph->g;
+    const uint32_t nq = (uint32_t)b->batched.size();
+    int truncated = 0;
+    if (nq) {
+        BatchRun run;
+        run.b = b;
+        run.cv = cv;
+        run.g = &g;
+        run.s = cv.stream;
+        run.nq = nq;
+        std::memset(&run.base, 0, sizeof(run.base));
+        run.base.plans = b->d_plans;
+        run.base.nq = nq;
+        run.base.seg = g.seg;
+        run.base.nbr = g.nbr;
+        run.base.V = g.V;
+        run.base.chunks_per_query = (g.V + 31) / 32;
+        run.base.table = cv.output;
+        run.base.qpos = b->d_qpos;
+        run.base.table_mode = b->table ? 1u : 0u;
+        run.base.heavy = cv.heavy;
+        run.base.heavy_cap = cv.heavy_cap;
+        run.base.piece_shift = b->piece_shift;
+        if ((uint64_t)nq * run.base.chunks_per_query >= (1ull << 32)) {
+            set_error("too many (query, root chunk) pairs in one batch; split the batch");
+            return FM_ERR_UNSUPPORTED;
+        }
+        FM_TRY(run.run(true));
+        for (uint32_t i = 0; i < nq; i++) {
+            const uint32_t qi = b->batched[i];
+            b->counts[qi] = b->h_qpos[i];
+            if (b->table && b->h_qpos[i] > b->table_cap[i]) truncated = 1;
+        }
+    }
+    for (uint32_t qi = 0; qi < b->n; qi++)
+        if (b->impossible[qi]) b->counts[qi] = 0;
+    // queries matched one by one (q == 1, or a graph with duplicate e-lines)
+    b->single_counts.clear();
+    for (uint32_t qi : b->single) {
+        fm_match_opts o;
+        fm_match_opts_default(&o);
+        o.mode = FM_MODE_COUNT;
+        fm_result r;
+        fm_status st = fm_match(b->ctx, b->graph, b->queries[qi], &o, &r);
+        if (st != FM_OK) return st;
+        b->counts[qi] = r.count;
+        b->launches += r.launches;
+    }
+    if (counts)
+        for (uint32_t i = 0; i < b->n; i++) counts[i] = b->counts[i];
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->launches = b->launches - launches0;
+        stats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        stats->batched_queries = nq;
+        stats->single_queries = (uint32_t)b->single.size();
+        stats->piece_shift = b->piece_shift;
+        stats->grid_quarters = b->sm_fraction;
+        for (uint32_t i = 0; i < b->n; i++) stats->embeddings += b->counts[i];
+    }
+    if (truncated) {
+        set_error("a query's table region overflowed; counts are exact");
+        return FM_ERR_OUTPUT_OVERFLOW;
+    }
+    return FM_OK;
+}
+
+fm_status fm_batch_rows(const fm_batch* b, uint32_t i, const uint32_t** rows_device, uint64_t* rows) {
+    if (!b || i >= b->n || !rows_device || !rows) return FM_ERR_ARG;
+    *rows_device = nullptr;
+    *rows = 0;
+    if (!b->table) return FM_OK;
+    for (size_t k = 0; k < b->batched.size(); k++) {
+        if (b->batched[k] != i) continue;
+        ContextView cv = context_view(b->ctx);
+        *rows_device = cv.output + b->table_base[k];
+        *rows = std::min<uint64_t>(b->counts[i], b->table_cap[k]);
+        return FM_OK;
+    }
+    set_error("this query was matched on its own (no batch table region)");
+    return FM_ERR_ARG;
+}
+
+fm_status fm_batch_copy_rows(const fm_batch* b, uint32_t i, uint32_t* host, uint64_t cap, uint64_t* copied) {
+    if (!copied || (cap && !host)) return FM_ERR_ARG;
+    *copied = 0;
+    const uint32_t* rows_device = nullptr;
+    uint64_t rows = 0;
+    FM_TRY(fm_batch_rows(b, i, &rows_device, &rows));
+    const uint64_t n = std::min(rows, cap);
+    if (n) {
+        ContextView cv = context_view(b->ctx);
+        FM_CUDA(cudaMemcpyAsync(host, rows_device, n * b->queries[i]->p.q * 4, cudaMemcpyDeviceToHost, cv.stream));
+        FM_CUDA(cudaStreamSynchronize(cv.stream));
+    }
+    *copied = n;
+    return FM_OK;
+}
+
+fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
+    if (!b) return FM_ERR_ARG;
+    // Search the split granularity (heavy piece size, the intersection tile a
+    // warp walks) and the grid of the main pass (warps in flight per query
+    // level); keep the fastest.  Each configuration runs the whole batch.
+    const uint32_t shifts[] = {0, 1, 2};
+    const uint32_t quarters[] = {2, 4};
+    double best_ms = -1;
+    uint32_t bs = b->piece_shift, bq = b->sm_fraction;
+    for (uint32_t sh : shifts) {
+        for (uint32_t qu : quarters) {
+            b->piece_shift = sh;
+            b->sm_fraction = qu;
+            if (b->exec) {
+                cudaGraphExecDestroy(b->exec);
+                b->exec = nullptr;
+            }
+            fm_batch_stats st;
+            fm_status s = fm_batch_run(b, nullptr, &st);   // builds the graph
+            if (s != FM_OK && s != FM_ERR_OUTPUT_OVERFLOW) return s;
+            s = fm_batch_run(b, nullptr, &st);             // timed replay
+            if (s != FM_OK && s != FM_ERR_OUTPUT_OVERFLOW) return s;
+            if (best_ms < 0 || st.wall_ms < best_ms) {
+                best_ms = st.wall_ms;
+                bs = sh;
+                bq = qu;
+            }
+        }
+    }
+    b->piece_shift = bs;
+    b->sm_fraction = bq;
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (best) {
+        std::memset(best, 0, sizeof(*best));
+        best->wall_ms = best_ms;
+        best->piece_shift = bs;
+        best->grid_quarters = bq;
+    }
+    return FM_OK;
+}
+
+}  // extern "C"

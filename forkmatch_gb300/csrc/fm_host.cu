@@ -729,3 +729,21 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     }
     return FM_OK;
 }
+
+fm::ContextView fm::context_view(fm_context* c) {
+    ContextView v;
+    v.device = c->device;
+    v.sms = c->sms;
+    v.stream = c->stream;
+    v.soln = c->soln;
+    v.soln_bytes = c->soln_bytes;
+    v.output = c->output;
+    v.output_bytes = c->output_bytes;
+    v.ctl = c->ctl;
+    v.h_ctl = c->h_ctl;
+    v.defs = c->defs;
+    v.def_cap = c->def_cap;
+    v.heavy = c->heavy;
+    v.heavy_cap = c->heavy_cap;
+    return v;
+}

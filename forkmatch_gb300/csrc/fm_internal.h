@@ -169,6 +169,23 @@ cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups
 size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps);
 int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block);
 
+// The parts of a context other translation units use (fm_host.cu owns it).
+struct ContextView {
+    int device, sms;
+    cudaStream_t stream;
+    char* soln;
+    uint64_t soln_bytes;
+    uint32_t* output;
+    uint64_t output_bytes;
+    LaunchCtl* ctl;        // one per depth
+    LaunchCtl* h_ctl;      // pinned mirror, one per depth
+    uint32_t* defs;
+    uint32_t def_cap;
+    HeavyEntry* heavy;
+    uint32_t heavy_cap;
+};
+ContextView context_view(fm_context* c);
+
 // Device graph build from device edge arrays (fm_graph.cu).
 fm_status build_device_graph(DeviceGraph& g, uint32_t V, uint32_t L, uint64_t E, const uint32_t* d_src,
                              const uint32_t* d_dst, const uint32_t* d_lab, cudaStream_t s);

@@ -36,49 +36,21 @@
 // `stop`, and exits; the host drains the output level (depth first) and
 // relaunches this level on the deferred chunks plus the unclaimed remainder.
 // Nothing spins and nothing traps.
-#include "fm_internal.h"
+#include "fm_device.cuh"
 
 namespace fm {
 namespace {
 
+using dev::kFull;
+using dev::ldg4;
+using dev::lower_bound_g;
+using dev::seg_at;
+using dev::seg_has;
+using dev::slot_locate;
+
 constexpr int kWarps = 8;
-constexpr unsigned kFull = 0xffffffffu;
 constexpr uint32_t kStage = 512;           // staged survivors per warp
 constexpr uint32_t kHeavyMaxPieces = 65536;
-
-__device__ __forceinline__ uint4 ldg4(const uint4* p) { return __ldg(p); }
-
-__device__ __forceinline__ uint32_t seg_at(const uint4& s, uint32_t t, const uint32_t* __restrict__ nbr) {
-    if (s.x <= 3) return t == 0 ? s.y : (t == 1 ? s.z : s.w);
-    return __ldg(nbr + (uint64_t)s.y * 4 + t);
-}
-
-// lower_bound of x in a[0, n)
-__device__ __forceinline__ uint32_t lower_bound_g(const uint32_t* __restrict__ a, uint32_t n, uint32_t x) {
-    uint32_t lo = 0;
-    while (n > 0) {
-        const uint32_t half = n >> 1;
-        if (__ldg(a + lo + half) < x) {
-            lo += half + 1;
-            n -= half + 1;
-        } else {
-            n = half;
-        }
-    }
-    return lo;
-}
-
-// Does the list hold at least `need` copies of x?
-__device__ __forceinline__ bool seg_has(const uint4& s, uint32_t x, uint32_t need, const uint32_t* __restrict__ nbr) {
-    if (s.x <= 3) {
-        const uint32_t c = (s.x > 0 && s.y == x) + (s.x > 1 && s.z == x) + (s.x > 2 && s.w == x);
-        return c >= need;
-    }
-    if (x < s.z || x > s.w) return false;
-    const uint32_t* a = nbr + (uint64_t)s.y * 4;
-    const uint32_t pos = lower_bound_g(a, s.x, x) + need - 1;
-    return pos < s.x && __ldg(a + pos) == x;
-}
 
 // Rank of position t within its run of equal values.
 __device__ __forceinline__ uint32_t seg_rank(const uint4& s, uint32_t t, uint32_t x, const uint32_t* __restrict__ nbr) {
@@ -133,16 +105,6 @@ __device__ __forceinline__ void defer_chunk(const ExpandParams& P, uint32_t chun
     const unsigned idx = atomicAdd(&P.ctl->ndef, 1u);
     if (idx < P.def_cap) P.def_out[idx] = chunk;
     else atomicOr(&P.ctl->error, 1u);
-}
-
-// Slot s of the warp's chunk belongs to parent j (the last j with excl[j] <= s),
-// at position t of that parent's driver list.
-__device__ __forceinline__ void slot_locate(uint32_t s, const uint32_t* excl_s, uint32_t& j, uint32_t& t) {
-    j = 0;
-#pragma unroll
-    for (uint32_t step = 16; step; step >>= 1)
-        if (excl_s[j + step] <= s) j += step;
-    t = s - excl_s[j];
 }
 
 // Does driver value x (position t of parent j's driver list dj) survive?

@@ -201,6 +201,37 @@ typedef struct fm_result {
 fm_status fm_match(fm_context* ctx, const fm_graph* g, const fm_query* q,
                    const fm_match_opts* opts, fm_result* out);
 
+/* Batched matching.  No counterpart in the reference, which matches one query
+ * per program run (src/smsm.cu:1182-1349): a batch matches many compiled
+ * queries against one resident graph in shared level launches (max(q) - 1 of
+ * them, captured once as a CUDA graph and replayed), each query's results
+ * identical to fm_match's.  Table mode gives every query an equal share of
+ * OUTPUT_PREALLOC (FM_ERR_OUTPUT_OVERFLOW if one overflows; counts stay
+ * exact).  Queries with one vertex, and every query on a graph with duplicate
+ * e-lines, are matched one by one through fm_match (count only). */
+typedef struct fm_batch fm_batch;
+typedef struct fm_batch_stats {
+    uint64_t embeddings;        /* sum of the counts */
+    uint64_t launches;          /* kernel launches of the run */
+    double wall_ms;             /* host wall time of fm_batch_run */
+    uint32_t batched_queries;   /* queries in the shared launches */
+    uint32_t single_queries;    /* queries matched one by one */
+    uint32_t piece_shift;       /* tuned: split-piece size = base << piece_shift */
+    uint32_t grid_quarters;     /* tuned: main-pass grid in quarters of a full grid */
+} fm_batch_stats;
+
+fm_status fm_batch_create(fm_context* ctx, const fm_graph* g, const fm_query* const* queries, uint32_t n,
+                          int32_t mode, fm_batch** out);
+fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats);
+/* Device table of query i after fm_batch_run (table mode): rows of q u32. */
+fm_status fm_batch_rows(const fm_batch* b, uint32_t i, const uint32_t** rows_device, uint64_t* rows);
+/* Copy query i's table to host memory (up to cap rows). */
+fm_status fm_batch_copy_rows(const fm_batch* b, uint32_t i, uint32_t* host, uint64_t cap, uint64_t* copied);
+/* Autotuner: runs the batch under each candidate split granularity and grid
+ * size, keeps the fastest for later runs. */
+fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best);
+void fm_batch_free(fm_batch* b);
+
 /* Matching that allocates nothing.  No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc at match time (an application whose
  * own pool owns all device memory and forbids stray allocations, or a
