@@ -456,7 +456,16 @@ struct fm_batch {
     uint32_t kmax[kMaxQ] = {};
     uint64_t level_cap = 0;
     uint32_t* level[kMaxQ] = {};
-    cudaGraphExec_t exec = nullptr;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};   // captured level sequence: count mode, table mode
+    std::vector<BatchPlan> h_plans;                  // host copy (table regions are resized)
+    bool regions_exact = false;                      // table regions sized from exact counts
+
+    void drop_graphs() {
+        for (auto& e : exec) {
+            if (e) cudaGraphExecDestroy(e);
+            e = nullptr;
+        }
+    }
     uint32_t piece_shift = 0;
     uint32_t sm_fraction = 4;             // quarters of the full grid used by the main pass
     std::vector<uint64_t> counts;
@@ -612,7 +621,8 @@ struct BatchRun {
     fm_status run(bool use_graph) {
         prepare();
         if (use_graph) {
-            if (!b->exec) {
+            cudaGraphExec_t& exec = b->exec[base.table_mode ? 1 : 0];
+            if (!exec) {
                 cudaGraph_t graph = nullptr;
                 FM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
                 fm_status st = enqueue_all();
@@ -622,11 +632,11 @@ struct BatchRun {
                     return st;
                 }
                 if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-                e = cudaGraphInstantiate(&b->exec, graph, 0);
+                e = cudaGraphInstantiate(&exec, graph, 0);
                 cudaGraphDestroy(graph);
                 if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
             }
-            FM_CUDA(cudaGraphLaunch(b->exec, s));
+            FM_CUDA(cudaGraphLaunch(exec, s));
         } else {
             FM_TRY(enqueue_all());
         }
@@ -739,6 +749,7 @@ fm_status fm_batch_create(fm_context* ctx, const fm_graph* graph, const fm_query
         }
         FM_CUDA(cudaMalloc(&b->d_plans, nq * sizeof(BatchPlan)));
         FM_CUDA(cudaMemcpy(b->d_plans, plans.data(), nq * sizeof(BatchPlan), cudaMemcpyHostToDevice));
+        b->h_plans = plans;
         FM_CUDA(cudaMalloc(&b->d_qpos, nq * sizeof(unsigned long long)));
         FM_CUDA(cudaHostAlloc(&b->h_qpos, nq * sizeof(unsigned long long), cudaHostAllocDefault));
     }
@@ -748,7 +759,7 @@ fm_status fm_batch_create(fm_context* ctx, const fm_graph* graph, const fm_query
 
 void fm_batch_free(fm_batch* b) {
     if (!b) return;
-    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->drop_graphs();
     if (b->d_plans) cudaFree(b->d_plans);
     if (b->d_qpos) cudaFree(b->d_qpos);
     if (b->h_qpos) cudaFreeHost(b->h_qpos);
@@ -780,7 +791,6 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
         run.base.chunks_per_query = (g.V + 31) / 32;
         run.base.table = cv.output;
         run.base.qpos = b->d_qpos;
-        run.base.table_mode = b->table ? 1u : 0u;
         run.base.heavy = cv.heavy;
         run.base.heavy_cap = cv.heavy_cap;
         run.base.piece_shift = b->piece_shift;
@@ -788,6 +798,27 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
             set_error("too many (query, root chunk) pairs in one batch; split the batch");
             return FM_ERR_UNSUPPORTED;
         }
+        if (b->table && !b->regions_exact) {
+            // First table run: count every query, then give each query a table
+            // region of exactly its size (in order, while OUTPUT_PREALLOC lasts).
+            run.base.table_mode = 0;
+            FM_TRY(run.run(true));
+            const uint64_t words = cv.output_bytes / 4;
+            uint64_t off = 0;
+            for (uint32_t i = 0; i < nq; i++) {
+                BatchPlan& bp = b->h_plans[i];
+                const uint64_t need = b->h_qpos[i] * bp.q;
+                bp.table_base = off;
+                bp.table_cap = off + need <= words ? b->h_qpos[i] : 0;
+                off += bp.table_cap * bp.q;
+                b->table_base[i] = bp.table_base;
+                b->table_cap[i] = bp.table_cap;
+            }
+            FM_CUDA(cudaMemcpyAsync(b->d_plans, b->h_plans.data(), nq * sizeof(BatchPlan), cudaMemcpyHostToDevice,
+                                    cv.stream));
+            b->regions_exact = true;
+        }
+        run.base.table_mode = b->table ? 1u : 0u;
         FM_TRY(run.run(true));
         for (uint32_t i = 0; i < nq; i++) {
             const uint32_t qi = b->batched[i];
@@ -873,10 +904,7 @@ fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
         for (uint32_t qu : quarters) {
             b->piece_shift = sh;
             b->sm_fraction = qu;
-            if (b->exec) {
-                cudaGraphExecDestroy(b->exec);
-                b->exec = nullptr;
-            }
+            b->drop_graphs();
             fm_batch_stats st;
             fm_status s = fm_batch_run(b, nullptr, &st);   // builds the graph
             if (s != FM_OK && s != FM_ERR_OUTPUT_OVERFLOW) return s;
@@ -891,10 +919,7 @@ fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
     }
     b->piece_shift = bs;
     b->sm_fraction = bq;
-    if (b->exec) {
-        cudaGraphExecDestroy(b->exec);
-        b->exec = nullptr;
-    }
+    b->drop_graphs();
     if (best) {
         std::memset(best, 0, sizeof(*best));
         best->wall_ms = best_ms;

@@ -61,7 +61,8 @@ def test_batch_counts_equal_single_and_oracle(env):
         counts, st = b.run()
         assert counts == want
         assert st.batched_queries == len(queries)
-    assert st.launches <= 2 * (max(q.q for q in queries) - 1) + 2
+    # shared levels: far fewer launches than matching the queries one by one
+    assert st.launches < sum(2 * (q.q - 1) for q in queries) // 4
     b.close()
 
 
