@@ -423,6 +423,7 @@ typedef struct {
     mctx* m;
     uint32_t f[ORA_MAXQ];
     ora_stats st;
+    uint64_t nodes;              /* search-tree nodes visited (for the limit) */
 } wctx;
 
 static uint64_t lower_b(const uint32_t* a, uint64_t n, uint32_t x) {
@@ -436,12 +437,13 @@ static void dfs(wctx* w, int d) {
     const ora_graph* g = w->m->g;
     int q = P->q;
     if (__atomic_load_n(&w->m->aborted, __ATOMIC_RELAXED)) return;
+    if (w->m->limit && (++w->nodes & 4095) == 0) {
+        /* the limit bounds the search: every node of the search tree counts */
+        uint64_t s = __atomic_add_fetch(&w->m->seen, 4096, __ATOMIC_RELAXED);
+        if (s > w->m->limit) __atomic_store_n(&w->m->aborted, 1, __ATOMIC_RELAXED);
+    }
     if (d == q) {
         w->st.count++;
-        if (w->m->limit && (w->st.count & 4095) == 0) {
-            uint64_t s = __atomic_add_fetch(&w->m->seen, 4096, __ATOMIC_RELAXED);
-            if (s > w->m->limit) __atomic_store_n(&w->m->aborted, 1, __ATOMIC_RELAXED);
-        }
         if (w->m->rows) {
             uint64_t idx = __atomic_fetch_add(&w->m->rows_next, 1, __ATOMIC_RELAXED);
             if (idx < w->m->rows_cap) {

@@ -63,7 +63,7 @@ enum {
     ORA_EXIT_QUERY_INVALID = 233,
     ORA_EXIT_QUERY_MISSING_DATA = 234,
     ORA_EXIT_NO_IDENTITY = 999,
-    ORA_EXIT_LIMIT = 1000     /* ora_match stopped at its embedding limit */
+    ORA_EXIT_LIMIT = 1000     /* ora_match stopped at its search limit */
 };
 
 /* Build from directed e-lines (both directions must be listed by the caller,
@@ -117,8 +117,9 @@ typedef struct {
  *                 then NOT multiplied (caller multiplies by sym_count).
  *   rows/rows_cap: optional table in reference column order.
  *   threads: worker threads (roots are claimed in chunks).
- *   limit: stop early (returning ORA_EXIT_LIMIT) once more than `limit`
- *          embeddings were found; 0 = no limit. */
+ *   limit: stop early (returning ORA_EXIT_LIMIT) once the search has
+ *          visited more than `limit` nodes (partial matches and embeddings);
+ *          0 = no limit. */
 int ora_match(const ora_graph* g, const ora_plan* p, int ref_symmetry,
               uint32_t root_begin, uint32_t root_end, int threads,
               uint32_t* rows, uint64_t rows_cap, uint64_t limit, ora_stats* st);

@@ -133,8 +133,8 @@ def plan(text, enumerate_aut=None):
 
 def match(graph, p, ref_symmetry=False, roots=None, threads=None, table=False, table_cap=None, limit=0):
     """Enumerate embeddings.  Returns (count, rows or None, Stats).
-    With ``limit`` > 0, raises OracleError(1000) once more than ``limit``
-    embeddings were found."""
+    With ``limit`` > 0, raises OracleError(1000) once the search visited more
+    than ``limit`` nodes (partial matches and embeddings)."""
     V = graph.V
     rb, re_ = (0, V) if roots is None else roots
     if threads is None:
