@@ -35,7 +35,7 @@ EXPORTS = [
     "fm_graph_free", "fm_query_compile_file", "fm_query_compile_text", "fm_query_get_info", "fm_query_free",
     "fm_match_opts_default", "fm_match", "fm_host_alloc", "fm_host_free", "fm_version", "fm_device_count",
     "fm_match_static", "fm_batch_create", "fm_batch_run", "fm_batch_rows", "fm_batch_copy_rows", "fm_batch_tune",
-    "fm_batch_free",
+    "fm_batch_free", "fm_batch_copy_tables",
 ]
 
 
@@ -126,6 +126,7 @@ def lib():
         L.fm_batch_run.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(BatchStats)]
         L.fm_batch_rows.argtypes = [vp, u32, ctypes.POINTER(vp), ctypes.POINTER(u64)]
         L.fm_batch_copy_rows.argtypes = [vp, u32, vp, u64, ctypes.POINTER(u64)]
+        L.fm_batch_copy_tables.argtypes = [vp, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]
         L.fm_batch_tune.argtypes = [vp, ctypes.POINTER(BatchStats)]
         L.fm_batch_free.argtypes = [vp]
         _lib = L
@@ -335,6 +336,21 @@ class Batch:
         n = ctypes.c_uint64()
         _check(lib().fm_batch_copy_rows(self._h, i, buf.ctypes.data, max_rows, ctypes.byref(n)), "fm_batch_copy_rows")
         return buf[: n.value * q].reshape(-1, q)
+
+    def copy_tables(self, host):
+        """Copy every table into ``host`` (a PinnedRows or a uint32 numpy
+        array) with one device-to-host copy.  Returns (words, offsets):
+        offsets[i] is the word offset of query i's rows, or None."""
+        n = len(self.queries)
+        offs = (ctypes.c_uint64 * max(1, n))()
+        words = ctypes.c_uint64()
+        if isinstance(host, PinnedRows):
+            ptr, cap = host.ptr, host.cap * host.q
+        else:
+            assert host.dtype == np.uint32 and host.flags["C_CONTIGUOUS"]
+            ptr, cap = host.ctypes.data, host.size
+        _check(lib().fm_batch_copy_tables(self._h, ptr, cap, offs, ctypes.byref(words)), "fm_batch_copy_tables")
+        return words.value, [None if offs[i] == (1 << 64) - 1 else int(offs[i]) for i in range(n)]
 
     def tune(self):
         st = BatchStats()

@@ -31,6 +31,8 @@ struct BatchPlan {                    // per query, in device memory
     uint8_t col_depth[kMaxQ];         // depth whose vertex fills table column c
     uint64_t table_base;              // u32 offset of the query's table region
     uint64_t table_cap;               // rows
+    uint64_t root_off;                // roots: heads[root_off .. root_off + n_roots)
+    uint32_t n_roots;
 };
 
 struct BatchParams {
@@ -44,7 +46,8 @@ struct BatchParams {
     uint64_t pstride;
     uint64_t n_parents;                       // roots: nq * chunks_per_query * 32
     const unsigned long long* n_parents_dev;  // set: read on the device (fresh chunks only)
-    uint32_t chunks_per_query;                // roots: ceil(V / 32)
+    uint32_t chunks_per_query;                // roots: the longest root list, in 32-root chunks
+    const uint32_t* heads;                    // per-label root lists of the graph
     uint32_t depth;
     uint32_t kmax;                            // segment records per parent reserved in shared memory
     // work items
@@ -146,8 +149,9 @@ __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem
     uint32_t qid, pidx;
     if (ROOTS) {
         qid = chunk / P.chunks_per_query;
-        pidx = (chunk - qid * P.chunks_per_query) * 32 + lane;   // the root vertex
-        valid = qid < P.nq && pidx < P.V;
+        const uint32_t r = (chunk - qid * P.chunks_per_query) * 32 + lane;
+        valid = qid < P.nq && r < P.plans[qid].n_roots;
+        pidx = valid ? __ldg(P.heads + P.plans[qid].root_off + r) : 0u;   // the root vertex
         m.rows_s[lane] = pidx;
     } else {
         const uint64_t p = (uint64_t)chunk * 32 + lane;
@@ -508,6 +512,17 @@ void build_plan(const Plan& pl, const DeviceGraph& g, BatchPlan& bp, bool& impos
         const uint32_t col = q - 1 - ref_depth[order[d]];
         bp.col_depth[col] = (uint8_t)d;
     }
+    // roots: the vertices with an e-line of a depth-1 label (the shortest list)
+    bool first = true;
+    for (uint32_t i = 0; i < nreq[1] && !impossible; i++) {
+        const uint32_t l = rlab[1][i];
+        const uint64_t n = g.head_off[l + 1] - g.head_off[l];
+        if (first || n < bp.n_roots) {
+            bp.root_off = g.head_off[l];
+            bp.n_roots = (uint32_t)n;
+            first = false;
+        }
+    }
 }
 
 struct BatchRun {
@@ -788,7 +803,10 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
         run.base.seg = g.seg;
         run.base.nbr = g.nbr;
         run.base.V = g.V;
-        run.base.chunks_per_query = (g.V + 31) / 32;
+        uint32_t longest = 1;
+        for (const BatchPlan& bp : b->h_plans) longest = std::max(longest, bp.n_roots);
+        run.base.chunks_per_query = (longest + 31) / 32;
+        run.base.heads = g.heads;
         run.base.table = cv.output;
         run.base.qpos = b->d_qpos;
         run.base.heavy = cv.heavy;
@@ -888,6 +906,36 @@ fm_status fm_batch_copy_rows(const fm_batch* b, uint32_t i, uint32_t* host, uint
         FM_CUDA(cudaStreamSynchronize(cv.stream));
     }
     *copied = n;
+    return FM_OK;
+}
+
+fm_status fm_batch_copy_tables(const fm_batch* b, uint32_t* host, uint64_t cap_words, uint64_t* offsets,
+                               uint64_t* words) {
+    if (!b || !words || (cap_words && !host)) return FM_ERR_ARG;
+    *words = 0;
+    if (offsets)
+        for (uint32_t i = 0; i < b->n; i++) offsets[i] = UINT64_MAX;
+    if (!b->table || b->batched.empty()) return FM_OK;
+    // regions are laid out in batch order; the packed span ends after the last
+    // region that holds rows
+    uint64_t end = 0;
+    for (size_t k = 0; k < b->batched.size(); k++) {
+        const uint32_t qi = b->batched[k];
+        const uint64_t rows = std::min<uint64_t>(b->counts[qi], b->table_cap[k]);
+        if (offsets) offsets[qi] = b->table_base[k];
+        end = std::max<uint64_t>(end, b->table_base[k] + rows * b->queries[qi]->p.q);
+    }
+    if (end > cap_words) {
+        set_error("host buffer smaller than the batch tables");
+        return FM_ERR_OUTPUT_OVERFLOW;
+    }
+    if (end) {
+        ContextView cv = context_view(b->ctx);
+        FM_CUDA(cudaSetDevice(cv.device));
+        FM_CUDA(cudaMemcpyAsync(host, cv.output, end * 4, cudaMemcpyDeviceToHost, cv.stream));
+        FM_CUDA(cudaStreamSynchronize(cv.stream));
+    }
+    *words = end;
     return FM_OK;
 }
 

@@ -105,6 +105,18 @@ __global__ void k_copy_long(const uint64_t* __restrict__ keys, const uint32_t* _
     }
 }
 
+// Source vertex of each segment (segments are in (label, src) order) and the
+// number of segments per label.
+__global__ void k_seg_heads(const uint64_t* __restrict__ keys, const uint64_t* __restrict__ seg_start, uint64_t nseg,
+                            uint32_t vbits, uint32_t* __restrict__ heads, unsigned int* __restrict__ per_label) {
+    const uint64_t vmask = (1ull << vbits) - 1;
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < nseg; s += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[seg_start[s]];
+        heads[s] = (uint32_t)((k >> vbits) & vmask);
+        atomicAdd(per_label + (uint32_t)(k >> (2 * vbits)), 1u);
+    }
+}
+
 uint32_t bits_for(uint64_t x) {   // bits needed to store values 0..x
     uint32_t b = 1;
     while (b < 64 && (x >> b)) ++b;
@@ -224,9 +236,22 @@ fm_status build_device_graph(DeviceGraph& g, uint32_t V, uint32_t L, uint64_t E,
         k_copy_long<<<grid_for(E, sms), 256, 0, s>>>(sorted, incl.as<uint32_t>(), seg_start.as<uint64_t>(),
                                                     off16.as<uint64_t>(), nseg, E, vbits, g.nbr);
         FM_CUDA(cudaGetLastError());
+        DevBuf per_label;
+        FM_CUDA(cudaMalloc(&g.heads, nseg * 4));
+        FM_CUDA(cudaMalloc(&per_label.p, (size_t)L * 4));
+        FM_CUDA(cudaMemsetAsync(per_label.p, 0, (size_t)L * 4, s));
+        k_seg_heads<<<grid_for(nseg, sms), 256, 0, s>>>(sorted, seg_start.as<uint64_t>(), nseg, vbits, g.heads,
+                                                       per_label.as<unsigned int>());
+        FM_CUDA(cudaGetLastError());
+        std::vector<uint32_t> cnt(L);
+        FM_CUDA(cudaMemcpyAsync(cnt.data(), per_label.p, (size_t)L * 4, cudaMemcpyDeviceToHost, s));
         FM_CUDA(cudaStreamSynchronize(s));
+        g.head_off.assign(L + 1, 0);
+        for (uint32_t l = 0; l < L; l++) g.head_off[l + 1] = g.head_off[l] + cnt[l];
     } else {
         FM_CUDA(cudaMalloc(&g.nbr, 16));
+        FM_CUDA(cudaMalloc(&g.heads, 16));
+        g.head_off.assign(L + 1, 0);
     }
     unsigned int hflags[4] = {0, 0, 0, 0};
     unsigned long long nlong = 0;

@@ -207,8 +207,10 @@ void* fm_context_stream(fm_context* ctx) { return ctx ? (void*)ctx->stream : nul
 static void free_device_graph(DeviceGraph& g) {
     if (g.seg) cudaFree(g.seg);
     if (g.nbr) cudaFree(g.nbr);
+    if (g.heads) cudaFree(g.heads);
     g.seg = nullptr;
     g.nbr = nullptr;
+    g.heads = nullptr;
 }
 
 void fm_graph_free(fm_graph* g) {
@@ -301,7 +303,7 @@ fm_status fm_graph_get_info(const fm_graph* g, fm_graph_info* info) {
     info->nbr_words = d.nbr_words;
     info->max_list = d.max_len;
     info->has_duplicates = d.has_dups;
-    info->device_bytes = (uint64_t)d.L * d.V * 16 + d.nbr_words * 4;
+    info->device_bytes = (uint64_t)d.L * d.V * 16 + d.nbr_words * 4 + d.segments * 4;
     info->build_ms = d.build_ms;
     return FM_OK;
 }
@@ -692,6 +694,21 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         b.nbr = g.nbr;
         b.V = g.V;
         b.root_begin = rb;
+        // Over the full vertex range the roots are the vertices that have an
+        // e-line of a depth-1 label (the shortest such list): any other root
+        // fails its depth-1 lookup.  A partial range walks the range itself.
+        uint64_t n_roots = re - rb;
+        b.root_list = nullptr;
+        if (rb == 0 && re == g.V && !g.head_off.empty()) {
+            for (uint32_t i = 0; i < nreq[1]; i++) {
+                const uint32_t l = dp.req_label[dp.req_begin[1] + i];
+                const uint64_t n = g.head_off[l + 1] - g.head_off[l];
+                if (!b.root_list || n < n_roots) {
+                    b.root_list = g.heads + g.head_off[l];
+                    n_roots = n;
+                }
+            }
+        }
         b.table = table_ptr;
         b.table_cap = table_cap;
         b.table_vec4 = (q % 4 == 0 && ((uintptr_t)table_ptr % 16) == 0) ? 1u : 0u;
@@ -699,7 +716,7 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         b.tot = ctx->tot;
         b.heavy = ctx->heavy;
         b.heavy_cap = ctx->heavy_cap;
-        fm_status st = run.run(re - rb);
+        fm_status st = run.run(n_roots);
         if (st != FM_OK) return st;
     }
     FM_CUDA(cudaEventRecord(ctx->ev1, s));

@@ -42,6 +42,11 @@ struct DeviceGraph {
     uint64_t E = 0;
     uint4* seg = nullptr;      // L*V records, index label*V + v
     uint32_t* nbr = nullptr;   // out-of-line lists
+    // Source vertex of every non-empty segment, label-major: the vertices with
+    // at least one e-line of label l are heads[head_off[l] .. head_off[l+1]),
+    // ascending.  A matching's roots come from the list of a depth-1 label.
+    uint32_t* heads = nullptr;
+    std::vector<uint64_t> head_off;      // L + 1 entries (host)
     uint64_t nbr_words = 0;
     uint64_t segments = 0, long_segments = 0;
     uint32_t max_len = 0;
@@ -141,6 +146,7 @@ struct ExpandParams {
     // launched back to back without the host reading anything in between
     const unsigned long long* n_parents_dev;
     uint32_t root_begin;            // roots: parent p is vertex root_begin + p
+    const uint32_t* root_list;      // roots, when set: parent p is vertex root_list[p]
     uint32_t depth;                 // parent rows have `depth` entries; new vertex goes to column depth
     // work items
     const uint32_t* def_in;

@@ -154,7 +154,7 @@ __device__ __forceinline__ WarpMem warp_mem(unsigned char* smem_raw, uint32_t wa
 // Column c of parent p of the level being expanded.
 template <bool ROOTS>
 __device__ __forceinline__ uint32_t parent_col(const ExpandParams& P, uint32_t c, uint32_t p) {
-    if (ROOTS) return P.root_begin + p;
+    if (ROOTS) return P.root_list ? __ldg(P.root_list + p) : P.root_begin + p;
     return __ldg(P.pin + c * P.pstride + p);
 }
 
@@ -218,7 +218,7 @@ __device__ __forceinline__ uint32_t load_chunk(const ExpandParams& P, const Warp
     const uint64_t p = (uint64_t)chunk * 32 + lane;
     valid = p < n_parents;
     if (ROOTS) {
-        m.rows_s[lane] = P.root_begin + (uint32_t)p;
+        m.rows_s[lane] = !P.root_list ? P.root_begin + (uint32_t)p : valid ? __ldg(P.root_list + p) : 0u;
     } else {
         for (uint32_t c = 0; c < d; c++) m.rows_s[c * 32 + lane] = valid ? P.pin[c * P.pstride + p] : 0u;
     }

@@ -315,6 +315,67 @@ def _edge_label(G, a, b):
     return None
 
 
+def query_path_walk(G, k, rng, tries=200):
+    """Path of k vertices along a random walk of the data graph (labels copied)."""
+    indptr, nbr, lab = G.adjacency()
+    deg = np.diff(indptr)
+    cand = np.nonzero(deg > 0)[0]
+    for _ in range(tries):
+        cur = int(rng.choice(cand))
+        seen = [cur]
+        ok = True
+        while len(seen) < k:
+            row = nbr[indptr[cur]:indptr[cur + 1]]
+            fresh = [int(w) for w in row if int(w) not in seen]
+            if not fresh:
+                ok = False
+                break
+            cur = fresh[int(rng.integers(0, len(fresh)))]
+            seen.append(cur)
+        if ok:
+            edges = [(i, i + 1, _edge_label(G, seen[i], seen[i + 1])) for i in range(k - 1)]
+            q = Query(k, edges, vlab=[int(G.vlab[s]) for s in seen], name="path%d" % k)
+            q.source = seen
+            return q
+    return None
+
+
+def query_cycle_walk(G, k, rng, tries=200):
+    """Cycle of k vertices: a walk path closed by an edge to its start; when the
+    data graph has no such edge the closing label is drawn at random (the
+    query may then have no match)."""
+    p = query_path_walk(G, k, rng, tries)
+    if p is None:
+        return None
+    a, b = p.source[-1], p.source[0]
+    lab = _edge_label(G, a, b)
+    if lab is None:
+        lab = int(rng.integers(1, G.n_elabels + 1))
+    q = Query(k, p.edges + [(k - 1, 0, lab)], vlab=p.vlab, name="cycle%d" % k)
+    q.source = p.source
+    return q
+
+
+def query_star_sample(G, k, rng, tries=200):
+    """Star of k vertices: a centre of degree >= k-1 and k-1 of its neighbours
+    (labels copied)."""
+    indptr, nbr, lab = G.adjacency()
+    deg = np.diff(indptr)
+    cand = np.nonzero(deg >= k - 1)[0]
+    if len(cand) == 0:
+        return None
+    for _ in range(tries):
+        c = int(rng.choice(cand))
+        row = nbr[indptr[c]:indptr[c + 1]]
+        leaves = rng.choice(row, size=k - 1, replace=False)
+        edges = [(0, i + 1, _edge_label(G, c, int(w))) for i, w in enumerate(leaves)]
+        seen = [c] + [int(w) for w in leaves]
+        q = Query(k, edges, vlab=[int(G.vlab[s]) for s in seen], name="star%d" % k)
+        q.source = seen
+        return q
+    return None
+
+
 def query_random_walk(G, k, rng, min_density=0.0, max_density=1.0, tree=False, bias=0.0, tries=200):
     """Query extracted from the data graph by a seeded walk (so >= 1 match).
 

@@ -11,6 +11,15 @@ plain_at_scale (the headline workload):
     labels uniform over 32 (written 1..32), uint32 ids.  16 queries of 8
     vertices, matched one at a time with full uint32 embedding tables.
     The query set is recorded in tests/golden/workload_plain_at_scale.json.
+
+batched (the multi-query workload):
+    R-MAT(0.57, 0.19, 0.19, 0.05), 2^22 vertices, 64M distinct undirected
+    edges (128M directed e-lines), vertex labels uniform over 8, edge labels
+    uniform over 64, uint32 ids.  512 queries of 4-16 vertices (size uniform)
+    and mixed shape: paths, cycles, stars and random-walk-induced subgraphs of
+    edge density 0.3-0.8, each drawn from the graph with copied labels.  The
+    query set with per-query counts is recorded in
+    tests/golden/workload_batched.json.
 """
 import hashlib
 import json
@@ -25,6 +34,7 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 PLAIN_AT_SCALE = dict(scale=20, m=16_000_000, n_elabels=32, n_vlabels=4, seed=2, vlabel_seed=3)
 PLAIN_SMALL = dict(n=1000, m=2000, n_elabels=87, seed=1)
+BATCHED = dict(scale=22, m=64_000_000, n_elabels=64, n_vlabels=8, seed=5, vlabel_seed=6)
 
 
 def edge_hash(src, dst, lab):
@@ -38,6 +48,13 @@ def plain_at_scale_graph():
     p = PLAIN_AT_SCALE
     rng = np.random.default_rng(p["vlabel_seed"])
     vlab = S.zipf_labels(rng, 1 << p["scale"], p["n_vlabels"], s=1.2)
+    return S.rmat(p["scale"], p["m"], p["seed"], p["n_elabels"], vlab=vlab, n_vlabels=p["n_vlabels"])
+
+
+def batched_graph():
+    p = BATCHED
+    rng = np.random.default_rng(p["vlabel_seed"])
+    vlab = rng.integers(0, p["n_vlabels"], size=1 << p["scale"], dtype=np.uint32)
     return S.rmat(p["scale"], p["m"], p["seed"], p["n_elabels"], vlab=vlab, n_vlabels=p["n_vlabels"])
 
 

@@ -227,6 +227,14 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats);
 fm_status fm_batch_rows(const fm_batch* b, uint32_t i, const uint32_t** rows_device, uint64_t* rows);
 /* Copy query i's table to host memory (up to cap rows). */
 fm_status fm_batch_copy_rows(const fm_batch* b, uint32_t i, uint32_t* host, uint64_t cap, uint64_t* copied);
+/* Copy every table of the batch to host memory with one device-to-host copy
+ * (the regions are packed back to back).  host: cap_words u32.  offsets: n
+ * entries (or NULL); offsets[i] = u32 word offset of query i's first row in
+ * `host`, UINT64_MAX for a query without a batch table region (matched on its
+ * own).  *words = u32 words written.  FM_ERR_OUTPUT_OVERFLOW when cap_words is
+ * too small (nothing copied). */
+fm_status fm_batch_copy_tables(const fm_batch* b, uint32_t* host, uint64_t cap_words, uint64_t* offsets,
+                               uint64_t* words);
 /* Autotuner: runs the batch under each candidate split granularity and grid
  * size, keeps the fastest for later runs. */
 fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best);

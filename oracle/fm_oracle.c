@@ -30,6 +30,16 @@ uint64_t ora_graph_list(const ora_graph* g, uint32_t label, uint32_t v, const ui
     return g->off[k + 1] - g->off[k];
 }
 
+uint32_t ora_graph_sources(const ora_graph* g, uint32_t label) {
+    uint32_t n = 0;
+    if (label >= g->L) return 0;
+    for (uint32_t v = 0; v < g->V; v++) {
+        uint64_t k = (uint64_t)label * g->V + v;
+        n += g->off[k + 1] != g->off[k];
+    }
+    return n;
+}
+
 void ora_graph_free(ora_graph* g) {
     if (!g) return;
     free(g->off);

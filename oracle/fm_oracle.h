@@ -79,6 +79,8 @@ uint64_t ora_graph_edges(const ora_graph* g);
 uint32_t ora_graph_labels(const ora_graph* g);
 /* Neighbour list of (label, v): returns its length and sets *ptr. */
 uint64_t ora_graph_list(const ora_graph* g, uint32_t label, uint32_t v, const uint32_t** ptr);
+/* Vertices with a non-empty list of `label`. */
+uint32_t ora_graph_sources(const ora_graph* g, uint32_t label);
 
 typedef struct {
     int q;                          /* query vertices */

@@ -63,6 +63,8 @@ def lib():
         L.ora_graph_edges.restype = ctypes.c_uint64
         L.ora_graph_labels.argtypes = [vp]
         L.ora_graph_labels.restype = ctypes.c_uint32
+        L.ora_graph_sources.argtypes = [vp, ctypes.c_uint32]
+        L.ora_graph_sources.restype = ctypes.c_uint32
         L.ora_query_plan.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(Plan)]
         L.ora_match.argtypes = [vp, ctypes.POINTER(Plan), ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
                                 ctypes.c_int, vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(Stats)]
@@ -111,6 +113,10 @@ class Graph:
     @property
     def E(self):
         return lib().ora_graph_edges(self._h)
+
+    def sources(self, label):
+        """Vertices with at least one e-line of ``label``."""
+        return lib().ora_graph_sources(self._h, int(label))
 
     def __del__(self):
         if getattr(self, "_h", None):

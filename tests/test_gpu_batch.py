@@ -79,6 +79,25 @@ def test_batch_tables_equal_single(env):
     b.close()
 
 
+def test_batch_copy_tables_one_copy(env):
+    ctx, g, og, queries, texts, want = env
+    b = fm.Batch(ctx, g, queries, mode=fm.MODE_TABLE)
+    counts, _ = b.run()
+    words_needed = sum(c * q.q for c, q in zip(counts, queries))
+    small = np.zeros(max(1, words_needed - 1), dtype=np.uint32)
+    with pytest.raises(fm.FMError):
+        b.copy_tables(small)
+    host = fm.PinnedRows(words_needed + 8, 1)
+    words, offs = b.copy_tables(host)
+    assert words == words_needed
+    flat = host.array
+    for i, q in enumerate(queries):
+        assert offs[i] is not None
+        got = flat[offs[i]: offs[i] + counts[i] * q.q].reshape(-1, q.q)
+        assert np.array_equal(got, b.rows(i, counts[i]))
+    b.close()
+
+
 def test_batch_each_query_alone_and_in_the_mix(env):
     ctx, g, og, queries, texts, want = env
     for i in (0, 5, 11, len(queries) - 1):

@@ -47,15 +47,16 @@ def check_case(ctx, g, og, qtext, expect_count=None, table=True, max_rows=1 << 2
     # with the reference order the per-level work equals the oracle's exactly
     r = fm.match(ctx, g, q, mode=fm.MODE_COUNT, order=fm.ORDER_REFERENCE)
     assert r.count == oc
-    # depth 1: every root is expanded (the lookup itself is the reference's
-    # root filter, src/smsm.cu:835), so the counters cover all V roots
+    # depth 1: the roots are the vertices with an e-line of one depth-1 label
+    # (every other vertex fails the reference's root lookup, src/smsm.cu:835)
     if r.launches == 0:
         # a query label is absent from the graph: no launch is needed
         assert oc == 0
         return oc
     if p.q > 1:
-        assert r.level[1].parents == og.V
-        assert r.level[1].lookups == og.V * p.nreq[1]
+        with_label = [og.sources(p.req_label[1][i]) for i in range(p.nreq[1])]
+        assert r.level[1].parents == min(with_label)
+        assert r.level[1].lookups == min(with_label) * p.nreq[1]
     for d in range(2, p.q):
         assert r.level[d].lookups == ost.lookups[d], ("lookups", d)
         assert r.level[d].list_words == ost.list_words[d], ("list_words", d)
