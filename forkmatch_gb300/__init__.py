@@ -35,7 +35,8 @@ EXPORTS = [
     "fm_graph_free", "fm_query_compile_file", "fm_query_compile_text", "fm_query_get_info", "fm_query_free",
     "fm_match_opts_default", "fm_match", "fm_host_alloc", "fm_host_free", "fm_version", "fm_device_count",
     "fm_match_static", "fm_batch_create", "fm_batch_run", "fm_batch_rows", "fm_batch_copy_rows", "fm_batch_tune",
-    "fm_batch_free", "fm_batch_copy_tables",
+    "fm_batch_free", "fm_batch_copy_tables", "fm_server_create", "fm_server_submit", "fm_server_poll",
+    "fm_server_release", "fm_server_get_stats", "fm_server_destroy",
 ]
 
 
@@ -87,6 +88,24 @@ class BatchStats(ctypes.Structure):
                 ("piece_shift", ctypes.c_uint32), ("grid_quarters", ctypes.c_uint32)]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32), ("min_lease_bytes", ctypes.c_uint64),
+                ("max_lease_bytes", ctypes.c_uint64)]
+
+
+class ServeResult(ctypes.Structure):
+    _fields_ = [("done", ctypes.c_int32), ("status", ctypes.c_int32), ("count", ctypes.c_uint64),
+                ("rows_copied", ctypes.c_uint64), ("truncated", ctypes.c_int32), ("batch", ctypes.c_uint32),
+                ("lease_bytes", ctypes.c_uint64), ("attempts", ctypes.c_uint32), ("queue_ms", ctypes.c_double),
+                ("service_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("queued", ctypes.c_uint64),
+                ("running", ctypes.c_uint64), ("batches", ctypes.c_uint64), ("embeddings", ctypes.c_uint64),
+                ("pool_bytes", ctypes.c_uint64), ("pool_free", ctypes.c_uint64), ("pool_peak_used", ctypes.c_uint64)]
+
+
 _lib = None
 
 
@@ -129,6 +148,12 @@ def lib():
         L.fm_batch_copy_tables.argtypes = [vp, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]
         L.fm_batch_tune.argtypes = [vp, ctypes.POINTER(BatchStats)]
         L.fm_batch_free.argtypes = [vp]
+        L.fm_server_create.argtypes = [vp, vp, ctypes.POINTER(ServerOpts), ctypes.POINTER(vp)]
+        L.fm_server_submit.argtypes = [vp, vp, i32, vp, u64, ctypes.POINTER(u64)]
+        L.fm_server_poll.argtypes = [vp, u64, i32, ctypes.POINTER(ServeResult)]
+        L.fm_server_release.argtypes = [vp, u64]
+        L.fm_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+        L.fm_server_destroy.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -361,6 +386,59 @@ class Batch:
         if getattr(self, "_h", None):
             lib().fm_batch_free(self._h)
             self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Server:
+    """Request loop over a resident graph (fm_server_*): admission by lease
+    footprint against the context's slab, slots overlapping on the device,
+    count-mode requests batched at the head of the queue."""
+
+    def __init__(self, ctx, graph, slots=4, max_batch=1, min_lease_bytes=0, max_lease_bytes=0):
+        self.ctx, self.graph = ctx, graph
+        o = ServerOpts(slots, max_batch, min_lease_bytes, max_lease_bytes)
+        h = ctypes.c_void_p()
+        _check(lib().fm_server_create(ctx._h, graph._h, ctypes.byref(o), ctypes.byref(h)), "fm_server_create")
+        self._h = h
+        self._keep = {}
+
+    def submit(self, query, mode=MODE_COUNT, host_rows=None):
+        """Queue a query; table mode copies rows into ``host_rows`` (a
+        PinnedRows or a C-contiguous uint32 array).  Returns the ticket."""
+        ptr, cap = None, 0
+        if host_rows is not None:
+            if isinstance(host_rows, PinnedRows):
+                ptr, cap = host_rows.ptr, host_rows.cap
+            else:
+                assert host_rows.dtype == np.uint32 and host_rows.flags["C_CONTIGUOUS"]
+                ptr, cap = host_rows.ctypes.data, host_rows.size // max(1, query.q)
+        t = ctypes.c_uint64()
+        _check(lib().fm_server_submit(self._h, query._h, mode, ptr, cap, ctypes.byref(t)), "fm_server_submit")
+        if host_rows is not None:
+            self._keep[t.value] = host_rows
+        return t.value
+
+    def poll(self, ticket, wait_ms=-1):
+        r = ServeResult()
+        _check(lib().fm_server_poll(self._h, ticket, int(wait_ms), ctypes.byref(r)), "fm_server_poll")
+        return r
+
+    def release(self, ticket):
+        _check(lib().fm_server_release(self._h, ticket), "fm_server_release")
+        self._keep.pop(ticket, None)
+
+    def stats(self):
+        s = ServerStats()
+        _check(lib().fm_server_get_stats(self._h, ctypes.byref(s)), "fm_server_get_stats")
+        return s
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fm_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
 
     def __del__(self):
         self.close()

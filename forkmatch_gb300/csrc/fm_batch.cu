@@ -463,6 +463,8 @@ struct fm_batch {
     cudaGraphExec_t exec[2] = {nullptr, nullptr};   // captured level sequence: count mode, table mode
     std::vector<BatchPlan> h_plans;                  // host copy (table regions are resized)
     bool regions_exact = false;                      // table regions sized from exact counts
+    bool replay = true;                              // capture the level sequence as a CUDA graph
+    bool own_scratch = true;                         // d_plans, d_qpos, h_qpos allocated here
 
     void drop_graphs() {
         for (auto& e : exec) {
@@ -686,10 +688,10 @@ struct BatchRun {
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-fm_status fm_batch_create(fm_context* ctx, const fm_graph* graph, const fm_query* const* queries, uint32_t n,
-                          int32_t mode, fm_batch** out) {
+fm_status batch_create_impl(fm_context* ctx, const fm_graph* graph, const fm_query* const* queries, uint32_t n,
+                            int32_t mode, const BatchScratch* scr, fm_batch** out) {
     if (!ctx || !graph || !out || (n && !queries)) return FM_ERR_ARG;
     *out = nullptr;
     std::unique_ptr<fm_batch> b(new fm_batch());
@@ -702,6 +704,10 @@ fm_status fm_batch_create(fm_context* ctx, const fm_graph* graph, const fm_query
     b->impossible.assign(n, 0);
     const DeviceGraph& g = graph->g;
     ContextView cv = context_view(ctx);
+    if (cv.serving) {
+        set_error("the context's slab belongs to a server (fm_server_create)");
+        return FM_ERR_ARG;
+    }
     if (g.device != cv.device) {
         set_error("graph and context live on different devices");
         return FM_ERR_ARG;
@@ -762,22 +768,58 @@ fm_status fm_batch_create(fm_context* ctx, const fm_graph* graph, const fm_query
             b->level[d] = (uint32_t*)(cv.soln + loff);
             loff += 4ull * (d + 1) * cap;
         }
-        FM_CUDA(cudaMalloc(&b->d_plans, nq * sizeof(BatchPlan)));
-        FM_CUDA(cudaMemcpy(b->d_plans, plans.data(), nq * sizeof(BatchPlan), cudaMemcpyHostToDevice));
         b->h_plans = plans;
-        FM_CUDA(cudaMalloc(&b->d_qpos, nq * sizeof(unsigned long long)));
-        FM_CUDA(cudaHostAlloc(&b->h_qpos, nq * sizeof(unsigned long long), cudaHostAllocDefault));
+        if (scr) {
+            // caller-owned scratch: no allocation (a server must not call
+            // cudaMalloc/cudaFree while other slots run)
+            if (scr->d_bytes < batch_scratch_bytes(nq, true) || scr->h_bytes < batch_scratch_bytes(nq, false)) {
+                set_error("batch scratch too small");
+                return FM_ERR_ARG;
+            }
+            b->own_scratch = false;
+            b->d_plans = (BatchPlan*)scr->d;
+            b->d_qpos = (unsigned long long*)((char*)scr->d + ((nq * sizeof(BatchPlan) + 255) & ~(size_t)255));
+            b->h_qpos = (unsigned long long*)scr->h;
+            FM_CUDA(cudaMemcpyAsync(b->d_plans, b->h_plans.data(), nq * sizeof(BatchPlan), cudaMemcpyHostToDevice,
+                                    cv.stream));
+        } else {
+            FM_CUDA(cudaMalloc(&b->d_plans, nq * sizeof(BatchPlan)));
+            FM_CUDA(cudaMemcpy(b->d_plans, plans.data(), nq * sizeof(BatchPlan), cudaMemcpyHostToDevice));
+            FM_CUDA(cudaMalloc(&b->d_qpos, nq * sizeof(unsigned long long)));
+            FM_CUDA(cudaHostAlloc(&b->h_qpos, nq * sizeof(unsigned long long), cudaHostAllocDefault));
+        }
     }
     *out = b.release();
     return FM_OK;
 }
 
+}  // namespace
+
+size_t fm::batch_scratch_bytes(uint32_t n, bool device) {
+    if (!device) return (size_t)n * sizeof(unsigned long long);
+    return ((n * sizeof(BatchPlan) + 255) & ~(size_t)255) + (size_t)n * sizeof(unsigned long long);
+}
+
+fm_status fm::batch_create_scratch(fm_context* ctx, const fm_graph* graph, const fm_query* const* queries, uint32_t n,
+                                   int32_t mode, const BatchScratch& scratch, fm_batch** out) {
+    return batch_create_impl(ctx, graph, queries, n, mode, &scratch, out);
+}
+
+extern "C" {
+
+fm_status fm_batch_create(fm_context* ctx, const fm_graph* graph, const fm_query* const* queries, uint32_t n,
+                          int32_t mode, fm_batch** out) {
+    return batch_create_impl(ctx, graph, queries, n, mode, nullptr, out);
+}
+
 void fm_batch_free(fm_batch* b) {
     if (!b) return;
     b->drop_graphs();
-    if (b->d_plans) cudaFree(b->d_plans);
-    if (b->d_qpos) cudaFree(b->d_qpos);
-    if (b->h_qpos) cudaFreeHost(b->h_qpos);
+    if (b->own_scratch) {
+        if (b->d_plans) cudaFree(b->d_plans);
+        if (b->d_qpos) cudaFree(b->d_qpos);
+        if (b->h_qpos) cudaFreeHost(b->h_qpos);
+    }
     delete b;
 }
 
@@ -820,7 +862,7 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
             // First table run: count every query, then give each query a table
             // region of exactly its size (in order, while OUTPUT_PREALLOC lasts).
             run.base.table_mode = 0;
-            FM_TRY(run.run(true));
+            FM_TRY(run.run(b->replay));
             const uint64_t words = cv.output_bytes / 4;
             uint64_t off = 0;
             for (uint32_t i = 0; i < nq; i++) {
@@ -837,7 +879,7 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
             b->regions_exact = true;
         }
         run.base.table_mode = b->table ? 1u : 0u;
-        FM_TRY(run.run(true));
+        FM_TRY(run.run(b->replay));
         for (uint32_t i = 0; i < nq; i++) {
             const uint32_t qi = b->batched[i];
             b->counts[qi] = b->h_qpos[i];
@@ -908,6 +950,14 @@ fm_status fm_batch_copy_rows(const fm_batch* b, uint32_t i, uint32_t* host, uint
     *copied = n;
     return FM_OK;
 }
+
+}  // extern "C"
+
+void fm::batch_set_replay(fm_batch* b, bool replay) {
+    if (b) b->replay = replay;
+}
+
+extern "C" {
 
 fm_status fm_batch_copy_tables(const fm_batch* b, uint32_t* host, uint64_t cap_words, uint64_t* offsets,
                                uint64_t* words) {

@@ -56,6 +56,7 @@ struct fm_context {
     MatchTotals* h_tot = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> prof;
+    bool serving = false;       // a server owns the slab (fm_match/fm_batch refuse)
 };
 
 namespace {
@@ -68,7 +69,19 @@ uint64_t env_u64(const char* name, uint64_t dflt) {
     return (end && *end == 0) ? (uint64_t)x : dflt;
 }
 
-constexpr uint64_t kMiscBytes = 64ull << 20;
+// [0, 4 KiB) control blocks, [4 KiB, 48 MiB) deferred-chunk lists (two per
+// depth), [48 MiB, 64 MiB) heavy-chunk entries
+void set_misc(fm_context* c, char* misc) {
+    static_assert(kMaxQ * sizeof(LaunchCtl) <= 4096, "per-level control blocks must fit in 4 KiB");
+    c->ctl = (LaunchCtl*)misc;                 // one control block per depth
+    c->tot = (MatchTotals*)(misc + 4096);
+    c->defs = (uint32_t*)(misc + 8192);
+    c->def_cap = (uint32_t)(((48ull << 20) - 8192) / 4 / (2 * kMaxQ));
+    c->heavy = (HeavyEntry*)(misc + (48ull << 20));
+    c->heavy_cap = (uint32_t)((kContextMiscBytes - (48ull << 20)) / sizeof(HeavyEntry));
+}
+
+constexpr uint64_t kMiscBytes = kContextMiscBytes;
 
 }  // namespace
 
@@ -182,16 +195,7 @@ fm_status fm_context_create(const fm_knobs* knobs, fm_context** out) {
     c->soln = c->slab;
     c->output = (uint32_t*)(c->slab + ((k.soln_prealloc_bytes + 255) & ~255ull));
     // control blocks hold 64-bit atomics: keep them 256-byte aligned whatever PREALLOC is
-    char* misc = c->slab + ((k.prealloc_bytes - kMiscBytes) & ~255ull);
-    // [0, 4 KiB) control blocks, [4 KiB, 48 MiB) deferred-chunk lists (two per
-    // depth), [48 MiB, 64 MiB) heavy-chunk entries
-    static_assert(kMaxQ * sizeof(LaunchCtl) <= 4096, "per-level control blocks must fit in 4 KiB");
-    c->ctl = (LaunchCtl*)misc;                 // one control block per depth
-    c->tot = (MatchTotals*)(misc + 4096);
-    c->defs = (uint32_t*)(misc + 8192);
-    c->def_cap = (uint32_t)(((48ull << 20) - 8192) / 4 / (2 * kMaxQ));
-    c->heavy = (HeavyEntry*)(misc + (48ull << 20));
-    c->heavy_cap = (uint32_t)((kMiscBytes - (48ull << 20)) / sizeof(HeavyEntry));
+    set_misc(c.get(), c->slab + ((k.prealloc_bytes - kMiscBytes) & ~255ull));
     FM_CUDA(cudaHostAlloc(&c->h_ctl, kMaxQ * sizeof(LaunchCtl), cudaHostAllocDefault));
     FM_CUDA(cudaHostAlloc(&c->h_tot, sizeof(MatchTotals), cudaHostAllocDefault));
     FM_CUDA(cudaEventCreate(&c->ev0));
@@ -574,6 +578,10 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     std::memset(out, 0, sizeof(*out));
     const DeviceGraph& g = graph->g;
     const Plan& pl = query->p;
+    if (ctx->serving) {
+        set_error("the context's slab belongs to a server (fm_server_create)");
+        return FM_ERR_ARG;
+    }
     if (g.device != ctx->device) {
         set_error("graph and context live on different devices");
         return FM_ERR_ARG;
@@ -747,8 +755,45 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     return FM_OK;
 }
 
+fm_status fm::context_create_view(fm_context* owner, char* misc, fm_context** out) {
+    *out = nullptr;
+    std::unique_ptr<fm_context, void (*)(fm_context*)> c(new fm_context(), fm_context_destroy);
+    c->knobs = owner->knobs;
+    c->device = owner->device;
+    c->sms = owner->sms;
+    FM_CUDA(cudaSetDevice(c->device));
+    FM_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    set_misc(c.get(), misc);
+    FM_CUDA(cudaHostAlloc(&c->h_ctl, kMaxQ * sizeof(LaunchCtl), cudaHostAllocDefault));
+    FM_CUDA(cudaHostAlloc(&c->h_tot, sizeof(MatchTotals), cudaHostAllocDefault));
+    FM_CUDA(cudaEventCreate(&c->ev0));
+    FM_CUDA(cudaEventCreate(&c->ev1));
+    *out = c.release();
+    return FM_OK;
+}
+
+void fm::context_set_regions(fm_context* c, char* soln, uint64_t soln_bytes, uint32_t* output, uint64_t output_bytes) {
+    c->soln = soln;
+    c->soln_bytes = soln_bytes;
+    c->output = output;
+    c->output_bytes = output_bytes;
+}
+
+char* fm::context_slab(fm_context* c, uint64_t* bytes) {
+    *bytes = c->knobs.prealloc_bytes;
+    return c->slab;
+}
+
+bool fm::context_set_serving(fm_context* c, bool on) {
+    if (on && c->serving) return false;
+    c->serving = on;
+    return true;
+}
+
 fm::ContextView fm::context_view(fm_context* c) {
     ContextView v;
+    v.serving = c->serving;
+    v.bank_rows = c->knobs.bank_rows;
     v.device = c->device;
     v.sms = c->sms;
     v.stream = c->stream;

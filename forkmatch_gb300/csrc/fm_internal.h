@@ -177,6 +177,8 @@ int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block
 
 // The parts of a context other translation units use (fm_host.cu owns it).
 struct ContextView {
+    bool serving;          // a server owns the slab
+    uint32_t bank_rows;    // CurBankSize
     int device, sms;
     cudaStream_t stream;
     char* soln;
@@ -191,6 +193,33 @@ struct ContextView {
     uint32_t heavy_cap;
 };
 ContextView context_view(fm_context* c);
+
+// Serving (fm_serve.cpp): per-slot contexts whose regions point into the
+// owner's slab.  A view owns its stream, pinned mirrors and events, not its
+// memory: `misc` is kContextMiscBytes of device memory (256-byte aligned) for
+// its control blocks, deferred lists and heavy entries; the level and table
+// regions are set per request.
+constexpr uint64_t kContextMiscBytes = 64ull << 20;
+fm_status context_create_view(fm_context* owner, char* misc, fm_context** out);
+void context_set_regions(fm_context* c, char* soln, uint64_t soln_bytes, uint32_t* output, uint64_t output_bytes);
+char* context_slab(fm_context* c, uint64_t* bytes);
+bool context_set_serving(fm_context* c, bool on);   // false if already serving
+// Batches created by a server are run once: no CUDA-graph capture.
+void batch_set_replay(fm_batch* b, bool replay);
+// A batch on caller-owned scratch (plans and counts of n queries), so that
+// creating and freeing it allocates no device or pinned memory.
+struct BatchScratch {
+    void* d;
+    uint64_t d_bytes;
+    void* h;                // pinned
+    uint64_t h_bytes;
+};
+size_t batch_scratch_bytes(uint32_t n, bool device);
+fm_status batch_create_scratch(fm_context* ctx, const fm_graph* graph, const fm_query* const* queries, uint32_t n,
+                               int32_t mode, const BatchScratch& scratch, fm_batch** out);
+// Estimated partial matches per depth under the automatic matching order
+// (independent e-lines, label frequencies): the server's footprint model.
+void estimate_level_rows(const Plan& P, const DeviceGraph& g, double est[kMaxQ]);
 
 // Device graph build from device edge arrays (fm_graph.cu).
 fm_status build_device_graph(DeviceGraph& g, uint32_t V, uint32_t L, uint64_t E, const uint32_t* d_src,

@@ -495,4 +495,39 @@ void choose_order(const Plan& P, const DeviceGraph& g, uint32_t order[kMaxQ]) {
     }
 }
 
+void estimate_level_rows(const Plan& P, const DeviceGraph& g, double est[kMaxQ]) {
+    const uint32_t q = P.q;
+    for (uint32_t d = 0; d < kMaxQ; d++) est[d] = 0;
+    if (q == 0) return;
+    uint32_t order[kMaxQ];
+    choose_order(P, g, order);
+    const double V = (double)g.V;
+    auto avg = [&](uint32_t l) {
+        uint64_t c = l < g.label_count.size() ? g.label_count[l] : 0;
+        return V > 0 ? (double)c / V : 0.0;
+    };
+    bool matched[kMaxQ] = {};
+    matched[order[0]] = true;
+    double card = V;
+    est[0] = card;
+    for (uint32_t d = 1; d < q; d++) {
+        const uint32_t v = order[d];
+        double mn = 1e300, prod = 1.0;
+        for (const auto& e : P.rows) {
+            if (e.a != v || !matched[e.b]) continue;
+            const double a = avg(e.l);
+            if (a < mn) {
+                if (mn < 1e299) prod *= mn / V;
+                mn = a;
+            } else {
+                prod *= a / V;
+            }
+        }
+        if (mn > 1e299) mn = 0;
+        card *= mn * prod;
+        est[d] = card;
+        matched[v] = true;
+    }
+}
+
 }  // namespace fm

@@ -256,6 +256,58 @@ void fm_batch_free(fm_batch* b);
 fm_status fm_match_static(const fm_graph* g, const fm_query* q, uint32_t* rows_out, uint64_t rows_cap,
                           uint64_t* count_out, uint64_t* rows_written, void* stream);
 
+/* Serving: a request loop over one resident graph.  No counterpart in the
+ * reference, which matches one query per process (src/smsm.cu:1351-1393).
+ * The server takes over the context's PREALLOC slab as its pool: every
+ * request leases level buffers (and, in table mode, a table region) sized by
+ * its estimated footprint, and is admitted in arrival order as soon as its
+ * lease fits the free pool and a slot is idle.  Each slot is one host thread
+ * and one stream, so admitted requests overlap on the device; queued
+ * count-mode requests are taken together (up to max_batch) and matched in
+ * shared level launches (fm_batch).  A footprint that proves too small costs
+ * time, never results: level buffers defer and drain, and a truncated table
+ * is matched again with an exact lease.  While a server exists, fm_match and
+ * fm_batch_create on its context return FM_ERR_ARG. */
+typedef struct fm_server fm_server;
+typedef struct fm_server_opts {
+    uint32_t slots;             /* requests on the device at once; 0 = 4 */
+    uint32_t max_batch;         /* count-mode requests matched together; 0 or 1 = one at a time */
+    uint64_t min_lease_bytes;   /* smallest level-buffer lease; 0 = 256 MiB */
+    uint64_t max_lease_bytes;   /* largest lease of one request; 0 = a quarter of the pool */
+} fm_server_opts;
+typedef struct fm_serve_result {
+    int32_t done;               /* 0 = queued or running */
+    fm_status status;
+    uint64_t count;
+    uint64_t rows_copied;       /* table mode: rows copied to the caller's buffer */
+    int32_t truncated;          /* table mode: the caller's buffer was too small */
+    uint32_t batch;             /* requests that shared its launches (1 = alone) */
+    uint64_t lease_bytes;       /* pool bytes it held (last attempt) */
+    uint32_t attempts;          /* runs (a retry follows a lease that was too small) */
+    double queue_ms;            /* submit -> admitted */
+    double service_ms;          /* admitted -> done */
+    double latency_ms;          /* submit -> done */
+} fm_serve_result;
+typedef struct fm_server_stats {
+    uint64_t submitted, completed, queued, running;
+    uint64_t batches;           /* shared-launch groups run */
+    uint64_t embeddings;        /* sum of completed counts */
+    uint64_t pool_bytes, pool_free, pool_peak_used;
+} fm_server_stats;
+
+fm_status fm_server_create(fm_context* ctx, const fm_graph* g, const fm_server_opts* opts, fm_server** out);
+/* Queue a query (copied: it may be freed after the call).  Table mode copies
+ * the rows into host_rows (cap rows of q u32; pinned memory copies fastest). */
+fm_status fm_server_submit(fm_server* s, const fm_query* q, int32_t mode, uint32_t* host_rows, uint64_t host_rows_cap,
+                           uint64_t* ticket);
+/* Result of a ticket; wait_ms < 0 waits until done, 0 returns at once.  The
+ * result stays available until fm_server_release. */
+fm_status fm_server_poll(fm_server* s, uint64_t ticket, int32_t wait_ms, fm_serve_result* out);
+fm_status fm_server_release(fm_server* s, uint64_t ticket);
+fm_status fm_server_get_stats(fm_server* s, fm_server_stats* out);
+/* Finishes every queued request, then stops the slots and returns the slab. */
+void fm_server_destroy(fm_server* s);
+
 /* Pinned host memory helpers (cudaHostAlloc / cudaFreeHost). */
 void* fm_host_alloc(uint64_t bytes);
 void fm_host_free(void* p);
