@@ -422,8 +422,10 @@ typedef struct {
     uint32_t* rows;
     uint64_t rows_cap;
     uint64_t rows_next;          /* atomic */
-    uint64_t limit;              /* stop once this many embeddings were seen (0 = none) */
+    uint64_t limit;              /* stop after this many search nodes (0 = none) */
     uint64_t seen;               /* atomic, in steps of 4096 */
+    uint64_t scan_limit;         /* stop after this many driver-list candidates (0 = none) */
+    uint64_t scanned;            /* atomic */
     int aborted;                 /* atomic */
     pthread_mutex_t mu;
     ora_stats total;
@@ -434,6 +436,7 @@ typedef struct {
     uint32_t f[ORA_MAXQ];
     ora_stats st;
     uint64_t nodes;              /* search-tree nodes visited (for the limit) */
+    uint64_t scans;              /* candidates not yet added to m->scanned */
 } wctx;
 
 static uint64_t lower_b(const uint32_t* a, uint64_t n, uint32_t x) {
@@ -473,6 +476,18 @@ static void dfs(wctx* w, int d) {
         w->st.lookups[d]++;
         w->st.list_words[d] += ln[i];
         if (ln[i] < ln[drv]) drv = i;
+    }
+    if (w->m->scan_limit && k) {
+        /* the scan limit bounds the work a node does on its driver list */
+        w->scans += ln[drv];
+        if (w->scans >= 4096) {
+            uint64_t s = __atomic_add_fetch(&w->m->scanned, w->scans, __ATOMIC_RELAXED);
+            w->scans = 0;
+            if (s > w->m->scan_limit) {
+                __atomic_store_n(&w->m->aborted, 1, __ATOMIC_RELAXED);
+                return;
+            }
+        }
     }
     int sym = (w->m->ref_sym && P->sym_count > 1) ? P->last_sym[d] : 0;
     uint32_t bound = sym ? w->f[d - sym] : 0;
@@ -535,7 +550,7 @@ static void* worker(void* arg) {
 
 int ora_match(const ora_graph* g, const ora_plan* p, int ref_symmetry,
               uint32_t root_begin, uint32_t root_end, int threads,
-              uint32_t* rows, uint64_t rows_cap, uint64_t limit, ora_stats* st) {
+              uint32_t* rows, uint64_t rows_cap, uint64_t limit, uint64_t scan_limit, ora_stats* st) {
     mctx m;
     memset(&m, 0, sizeof(m));
     m.g = g; m.p = p; m.ref_sym = ref_symmetry;
@@ -544,6 +559,7 @@ int ora_match(const ora_graph* g, const ora_plan* p, int ref_symmetry,
     m.next_root = root_begin;
     m.rows = rows; m.rows_cap = rows_cap;
     m.limit = limit;
+    m.scan_limit = scan_limit;
     pthread_mutex_init(&m.mu, NULL);
     if (threads < 1) threads = 1;
     if (threads > 512) threads = 512;

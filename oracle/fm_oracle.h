@@ -63,7 +63,7 @@ enum {
     ORA_EXIT_QUERY_INVALID = 233,
     ORA_EXIT_QUERY_MISSING_DATA = 234,
     ORA_EXIT_NO_IDENTITY = 999,
-    ORA_EXIT_LIMIT = 1000     /* ora_match stopped at its search limit */
+    ORA_EXIT_LIMIT = 1000     /* ora_match stopped at one of its search limits */
 };
 
 /* Build from directed e-lines (both directions must be listed by the caller,
@@ -121,10 +121,12 @@ typedef struct {
  *   threads: worker threads (roots are claimed in chunks).
  *   limit: stop early (returning ORA_EXIT_LIMIT) once the search has
  *          visited more than `limit` nodes (partial matches and embeddings);
- *          0 = no limit. */
+ *          0 = no limit.
+ *   scan_limit: the same for the driver-list candidates the nodes scanned
+ *          (a node whose lists are long does work without making nodes). */
 int ora_match(const ora_graph* g, const ora_plan* p, int ref_symmetry,
               uint32_t root_begin, uint32_t root_end, int threads,
-              uint32_t* rows, uint64_t rows_cap, uint64_t limit, ora_stats* st);
+              uint32_t* rows, uint64_t rows_cap, uint64_t limit, uint64_t scan_limit, ora_stats* st);
 
 #ifdef __cplusplus
 }

@@ -67,7 +67,8 @@ def lib():
         L.ora_graph_sources.restype = ctypes.c_uint32
         L.ora_query_plan.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(Plan)]
         L.ora_match.argtypes = [vp, ctypes.POINTER(Plan), ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
-                                ctypes.c_int, vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(Stats)]
+                                ctypes.c_int, vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                ctypes.POINTER(Stats)]
         _lib = L
     return _lib
 
@@ -137,10 +138,12 @@ def plan(text, enumerate_aut=None):
     return p
 
 
-def match(graph, p, ref_symmetry=False, roots=None, threads=None, table=False, table_cap=None, limit=0):
+def match(graph, p, ref_symmetry=False, roots=None, threads=None, table=False, table_cap=None, limit=0,
+          scan_limit=0):
     """Enumerate embeddings.  Returns (count, rows or None, Stats).
     With ``limit`` > 0, raises OracleError(1000) once the search visited more
-    than ``limit`` nodes (partial matches and embeddings)."""
+    than ``limit`` nodes (partial matches and embeddings); ``scan_limit``
+    does the same for the driver-list candidates the nodes scanned."""
     V = graph.V
     rb, re_ = (0, V) if roots is None else roots
     if threads is None:
@@ -152,7 +155,8 @@ def match(graph, p, ref_symmetry=False, roots=None, threads=None, table=False, t
         rows = np.zeros((cap, p.q), dtype=np.uint32)
     st = Stats()
     rc = lib().ora_match(graph._h, ctypes.byref(p), int(bool(ref_symmetry)), rb, re_, int(threads),
-                         rows.ctypes.data if rows is not None else None, cap, int(limit), ctypes.byref(st))
+                         rows.ctypes.data if rows is not None else None, cap, int(limit), int(scan_limit),
+                         ctypes.byref(st))
     if rc:
         raise OracleError(rc, "ora_match")
     if rows is not None:

@@ -146,8 +146,10 @@ def main():
         for qname, qtext in queries:
             p = O.plan(qtext)
             try:
-                full, _, st = O.match(og, p, limit=2_000_000)
+                full, _, st = O.match(og, p, limit=1 << 32)
             except O.OracleError:
+                continue
+            if full > 2_000_000:
                 continue
             refc = O.ref_count(og, p)
             entries.append({"query": qname, "text": qtext.decode(), "count": int(full), "ref_count": int(refc),

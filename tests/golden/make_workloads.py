@@ -15,7 +15,23 @@ workload_plain_at_scale.json
     Counts are the oracle's exact full counts, so the benchmark doubles as a
     full-size bit-exact check.
 
-Usage: python tests/golden/make_workloads.py
+workload_batched.json
+    Graph: forkmatch_gb300.workloads.batched_graph().  512 query slots; slot i
+    asks for k = 4 + (i mod 13) vertices (sizes 4..16 uniform) and the shape
+    ("path", "cycle", "star", "walk")[(i // 13) mod 4].  Paths, cycles and
+    stars are drawn from a random walk / a sampled centre of the graph with
+    copied labels; "walk" is the induced subgraph of a hub-biased walk with
+    edge density in [0.3, 0.8].  A candidate is kept when the oracle finishes
+    it within 2^27 search nodes and its count is at most 2^22.
+    Each (shape, k) class is first probed with PROBE candidates; a class none
+    of whose candidates fits is recorded under "excluded" with the evidence
+    (search nodes exceeded, and the homomorphism count of the probe for paths
+    and stars, an upper bound that shows the size), and its slots take a
+    "walk" query of the same k instead.  On this graph (per-label degree 0.5
+    on average, hubs of degree 1.6e5) every path and star and every cycle of
+    more than 4 vertices falls in that case.
+
+Usage: python tests/golden/make_workloads.py [plain_at_scale|batched]
 """
 import json
 import os
@@ -31,14 +47,17 @@ from forkmatch_gb300 import synth as S  # noqa: E402
 from forkmatch_gb300 import workloads as W  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-LIMIT = 1 << 28
+
+def _oracle_graph(G):
+    src, dst, lab = G.directed()
+    return src, dst, lab, O.Graph.from_edges(G.V, G.n_elabels + 1, src, dst, lab)
 
 
-def main():
+def plain_at_scale():
+    limit = 1 << 28
     t0 = time.time()
     G = W.plain_at_scale_graph()
-    src, dst, lab = G.directed()
-    og = O.Graph.from_edges(G.V, G.n_elabels + 1, src, dst, lab)
+    src, dst, lab, og = _oracle_graph(G)
     print("graph %.1fs" % (time.time() - t0), flush=True)
     rng = np.random.default_rng(20261203)
     picked = {"dense": [], "sparse": []}
@@ -56,8 +75,10 @@ def main():
             p = O.plan(text, enumerate_aut=0)
             t = time.time()
             try:
-                c, _, st = O.match(og, p, limit=LIMIT)
+                c, _, st = O.match(og, p, limit=1 << 34)
             except O.OracleError:
+                c = limit + 1
+            if c > limit:
                 print(kind, "rejected (count > 2^28)", flush=True)
                 continue
             if c == 0:
@@ -74,5 +95,116 @@ def main():
     print("total embeddings", sum(q["count"] for q in out["queries"]), "%.1fs" % (time.time() - t0))
 
 
+SHAPES = ("path", "cycle", "star", "walk")
+SLOTS = 512
+NODE_LIMIT = 1 << 27
+COUNT_CAP = 1 << 22
+PROBE = 4
+
+
+def _draw(G, shape, k, rng):
+    if shape == "path":
+        return S.query_path_walk(G, k, rng)
+    if shape == "cycle":
+        return S.query_cycle_walk(G, k, rng)
+    if shape == "star":
+        return S.query_star_sample(G, k, rng)
+    return S.query_random_walk(G, k, rng, min_density=0.3, max_density=0.8, bias=3.0, tries=60)
+
+
+def _hom_estimate(G, q):
+    """Homomorphism count of a path or star query (float; an upper bound on
+    its embedding count): products of per-label adjacency matrices."""
+    import scipy.sparse as sp
+    src, dst, lab = G.directed()
+    mats = {}
+
+    def A(l):
+        if l not in mats:
+            m = lab == l
+            mats[l] = sp.csr_matrix((np.ones(int(m.sum())), (src[m], dst[m])), shape=(G.V, G.V))
+        return mats[l]
+    if q.name.startswith("star"):
+        acc = np.ones(G.V)
+        for _, _, l in q.edges:
+            acc *= np.asarray(A(l).sum(axis=1)).ravel()
+        return float(acc.sum())
+    v = np.ones(G.V)
+    for a, b, l in reversed(q.edges):
+        v = A(l) @ v
+    return float(v.sum())
+
+
+def _screen(og, q):
+    text = q.to_g_text()
+    p = O.plan(text, enumerate_aut=0)
+    t = time.time()
+    try:
+        c, _, _ = O.match(og, p, limit=NODE_LIMIT)
+    except O.OracleError:
+        return None, time.time() - t, text
+    return c, time.time() - t, text
+
+
+def batched():
+    t0 = time.time()
+    G = W.batched_graph()
+    src, dst, lab, og = _oracle_graph(G)
+    G.adjacency()
+    print("graph %.1fs" % (time.time() - t0), flush=True)
+    rng = np.random.default_rng(20261204)
+    feasible = {}
+    excluded = []
+    for shape in SHAPES[:3]:
+        for k in range(4, 17):
+            ok = False
+            notes = []
+            for _ in range(PROBE):
+                q = _draw(G, shape, k, rng)
+                if q is None:
+                    notes.append("no candidate")
+                    continue
+                c, sec, _ = _screen(og, q)
+                if c is not None and c <= COUNT_CAP:
+                    ok = True
+                    break
+                note = {"search_nodes": "> 2^27" if c is None else "finished", "count": c}
+                if shape != "cycle":
+                    note["homomorphisms"] = "%.3g" % _hom_estimate(G, q)
+                notes.append(note)
+            feasible[(shape, k)] = ok
+            if not ok:
+                excluded.append({"shape": shape, "k": k, "probes": notes})
+            print(shape, k, "feasible" if ok else "excluded", notes[-1:] if notes else "", flush=True)
+    queries = []
+    for i in range(SLOTS):
+        k = 4 + i % 13
+        want = SHAPES[(i // 13) % 4]
+        shape = want if want == "walk" or feasible[(want, k)] else "walk"
+        for attempt in range(400):
+            q = _draw(G, shape, k, rng)
+            if q is None:
+                continue
+            c, sec, text = _screen(og, q)
+            if c is None or c > COUNT_CAP:
+                continue
+            queries.append({"slot": i, "requested": want, "shape": shape, "k": k, "text": text.decode(),
+                            "edges": len(q.edges), "density": round(q.density, 4), "count": int(c),
+                            "oracle_seconds": round(sec, 3)})
+            print(i, want, shape, k, len(q.edges), "count", c, "%.2fs" % sec, flush=True)
+            break
+        else:
+            raise RuntimeError("slot %d (%s, k=%d): no candidate fits" % (i, shape, k))
+    out = {"workload": "batched", "params": W.BATCHED, "V": G.V, "E": int(len(src)),
+           "edge_sha256": W.edge_hash(src, dst, lab), "node_limit": NODE_LIMIT, "count_cap": COUNT_CAP,
+           "excluded": excluded, "queries": queries}
+    with open(os.path.join(HERE, "workload_batched.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    tot = sum(q["count"] for q in queries)
+    rows = sum(q["count"] * q["k"] * 4 for q in queries)
+    print("total embeddings", tot, "table bytes", rows, "%.1fs" % (time.time() - t0))
+
+
 if __name__ == "__main__":
-    main()
+    which = sys.argv[1] if len(sys.argv) > 1 else "plain_at_scale"
+    {"plain_at_scale": plain_at_scale, "batched": batched}[which]()

@@ -35,7 +35,7 @@ def _queries(G, og, rng, n=40, cap=1 << 20):
             continue
         t = q.to_g_text()
         try:
-            c, _, _ = O.match(og, O.plan(t, enumerate_aut=0), limit=1 << 24)
+            c, _, _ = O.match(og, O.plan(t, enumerate_aut=0), limit=1 << 22, scan_limit=1 << 26)
         except O.OracleError:
             continue
         if c <= cap:
@@ -47,13 +47,13 @@ def _queries(G, og, rng, n=40, cap=1 << 20):
 def env():
     from forkmatch_gb300 import build
     build.build()
-    G = S.rmat(13, 40000, seed=31, n_elabels=3)
+    G = S.rmat(13, 40000, seed=31, n_elabels=8)
     src, dst, lab = G.directed()
-    og = O.Graph.from_edges(G.V, 4, src, dst, lab)
+    og = O.Graph.from_edges(G.V, 9, src, dst, lab)
     texts = _queries(G, og, np.random.default_rng(32))
     ctx = fm.Context(prealloc_bytes=6 << 30, soln_prealloc_bytes=2 << 30, output_prealloc_bytes=2 << 30,
                      bank_rows=1024)
-    g = fm.Graph.from_edges(ctx, G.V, 4, src, dst, lab)
+    g = fm.Graph.from_edges(ctx, G.V, 9, src, dst, lab)
     queries = [fm.Query.from_text(t) for t in texts]
     # plain runs (before any server exists) and the oracle
     want = [fm.match(ctx, g, q, mode=fm.MODE_COUNT).count for q in queries]
@@ -152,7 +152,7 @@ def test_pool_admits_only_what_fits(env):
     G = env["G"]
     ctx = fm.Context(prealloc_bytes=8 * 64 * MB + 400 * MB, soln_prealloc_bytes=64 * MB, output_prealloc_bytes=64 * MB,
                      bank_rows=1024)
-    g = fm.Graph.from_edges(ctx, G.V, 4, env["src"], env["dst"], env["lab"])
+    g = fm.Graph.from_edges(ctx, G.V, 9, env["src"], env["dst"], env["lab"])
     srv = fm.Server(ctx, g, slots=8, min_lease_bytes=96 * MB, max_lease_bytes=96 * MB)
     try:
         st0 = srv.stats()
