@@ -402,3 +402,61 @@ def query_random_walk(G, k, rng, min_density=0.0, max_density=1.0, tree=False, b
             q.source = seen
             return q
     return None
+
+
+# ---------------------------------------------------------------- large graphs
+
+class BigAdjacency:
+    """Neighbour lists of a large LabeledGraph without sorting all e-lines:
+    the undirected edges are sorted by u (u < v), so the u-side lists are
+    slices, and one argsort of v gives the v-side lists.  Rows are unsorted."""
+
+    def __init__(self, G):
+        self.G = G
+        idx = np.arange(G.V + 1, dtype=np.int64)
+        self.out_ptr = np.searchsorted(G.u, idx)
+        order = np.argsort(G.v, kind="stable")
+        vs = G.v[order]
+        self.in_ptr = np.searchsorted(vs, idx)
+        self.in_src = G.u[order]
+        self.in_lab = G.lab[order]
+        self.deg = np.diff(self.out_ptr) + np.diff(self.in_ptr)
+
+    def neighbours(self, x):
+        a, b = self.out_ptr[x], self.out_ptr[x + 1]
+        c, d = self.in_ptr[x], self.in_ptr[x + 1]
+        return (np.concatenate([self.G.v[a:b], self.in_src[c:d]]),
+                np.concatenate([self.G.lab[a:b], self.in_lab[c:d]]))
+
+
+def query_walk_big(A, k, rng, tries=50):
+    """Induced subgraph of a k-vertex random walk (uniform start, uniform
+    steps) on a BigAdjacency, labels copied."""
+    G = A.G
+    for _ in range(tries):
+        start = int(rng.integers(0, G.V))
+        if A.deg[start] == 0:
+            continue
+        seen = [start]
+        cur = start
+        steps = 0
+        while len(seen) < k and steps < 30 * k:
+            steps += 1
+            nb, _ = A.neighbours(cur)
+            nxt = int(nb[rng.integers(0, len(nb))])
+            if nxt not in seen:
+                seen.append(nxt)
+            cur = nxt
+        if len(seen) < k:
+            continue
+        edges = []
+        for i in range(k):
+            nb, lb = A.neighbours(seen[i])
+            for j in range(i + 1, k):
+                m = nb == seen[j]
+                if m.any():
+                    edges.append((i, j, int(lb[m][0])))
+        q = Query(k, edges, vlab=[int(G.vlab[s]) for s in seen], name="walk%d" % k)
+        q.source = seen
+        return q
+    return None

@@ -20,6 +20,14 @@ batched (the multi-query workload):
     edge density 0.3-0.8, each drawn from the graph with copied labels.  The
     query set with per-query counts is recorded in
     tests/golden/workload_batched.json.
+
+serving (the request-loop workload):
+    R-MAT(0.57, 0.19, 0.19, 0.05), 2^24 vertices, 256M distinct undirected
+    edges (512M directed e-lines), vertex labels uniform over 8, edge labels
+    uniform over 64, uint32 ids, resident on the device.  Queries of 4-12
+    vertices are induced subgraphs of seeded random walks, screened on the
+    device (a root sample first, then the full count) so that every request
+    is an interactive one; arrivals are Poisson at swept rates.
 """
 import hashlib
 import json
@@ -35,6 +43,7 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 PLAIN_AT_SCALE = dict(scale=20, m=16_000_000, n_elabels=32, n_vlabels=4, seed=2, vlabel_seed=3)
 PLAIN_SMALL = dict(n=1000, m=2000, n_elabels=87, seed=1)
 BATCHED = dict(scale=22, m=64_000_000, n_elabels=64, n_vlabels=8, seed=5, vlabel_seed=6)
+SERVING = dict(scale=24, m=256_000_000, n_elabels=64, n_vlabels=8, seed=7, vlabel_seed=8)
 
 
 def edge_hash(src, dst, lab):
@@ -53,6 +62,15 @@ def plain_at_scale_graph():
 
 def batched_graph():
     p = BATCHED
+    rng = np.random.default_rng(p["vlabel_seed"])
+    vlab = rng.integers(0, p["n_vlabels"], size=1 << p["scale"], dtype=np.uint32)
+    return S.rmat(p["scale"], p["m"], p["seed"], p["n_elabels"], vlab=vlab, n_vlabels=p["n_vlabels"])
+
+
+def serving_graph(scale=None, m=None):
+    p = dict(SERVING)
+    if scale is not None:
+        p["scale"], p["m"] = scale, m
     rng = np.random.default_rng(p["vlabel_seed"])
     vlab = rng.integers(0, p["n_vlabels"], size=1 << p["scale"], dtype=np.uint32)
     return S.rmat(p["scale"], p["m"], p["seed"], p["n_elabels"], vlab=vlab, n_vlabels=p["n_vlabels"])
