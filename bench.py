@@ -239,7 +239,8 @@ def run_ours(args, rank, world, local):
     queries_meta = wl["queries"]
     max_count = max(q["count"] for q in queries_meta)
     out_bytes = ((int(max_count * 8 * 4 * 1.05) + (64 << 20)) >> 20) << 20
-    ctx = fm.Context(prealloc_bytes=24 * GB + out_bytes + (128 << 20), soln_prealloc_bytes=24 * GB,
+    # the slab beyond SOLN + OUTPUT is the pool of the served e2e path
+    ctx = fm.Context(prealloc_bytes=64 * GB, soln_prealloc_bytes=24 * GB,
                      output_prealloc_bytes=out_bytes, bank_rows=1 << 16, device=local)
     t = time.time()
     g = fm.Graph.from_edges(ctx, G.V, G.n_elabels + 1, src, dst, lab)
@@ -339,6 +340,46 @@ def run_ours(args, rank, world, local):
         el = time.perf_counter() - w0
         e2e_paths[name] = {"value": tot_e / el, "ms_per_step": 1000 * el / args.steps,
                            "h2d_bytes_per_step": hb, "d2h_bytes_per_step": db, "total": tot_e, "seconds": el}
+
+    # served: the queries as table requests to a server (fm_server_*) with
+    # three slots, so one request's table copy to the host overlaps the next
+    # one's matching; every table lands in its own slice of one pinned buffer
+    if world == 1:
+        qw = [c * qi.q for c, qi in zip(counts, qinfo)]
+        offs = np.concatenate([[0], np.cumsum(qw)]).astype(np.int64)
+        host = fm.PinnedRows(int(offs[-1]) + 1, 1)
+        views = [host.array[offs[i]:offs[i + 1]] for i in range(len(texts))]
+        srv = fm.Server(ctx, g, slots=3, min_lease_bytes=8 * GB, max_lease_bytes=16 * GB)
+
+        def e2e_served():
+            tickets = []
+            for tx, view in zip(texts, views):
+                q = fm.Query.from_text(tx)
+                tickets.append(srv.submit(q, mode=fm.MODE_TABLE, host_rows=view))
+                q.close()
+            c = d2h = 0
+            for t, qi in zip(tickets, qinfo):
+                r = srv.poll(t)
+                if r.status != fm.FM_OK:
+                    raise RuntimeError("served request failed with status %d" % r.status)
+                c += r.count
+                d2h += r.rows_copied * qi.q * 4
+                srv.release(t)
+            return c, sum(len(tx) for tx in texts), d2h
+
+        try:
+            e2e_served()
+            w0 = time.perf_counter()
+            tot_e = 0
+            for _ in range(args.steps):
+                c, hb, db = e2e_served()
+                tot_e += c
+            el = time.perf_counter() - w0
+        finally:
+            srv.close()
+        e2e_paths["served_overlap"] = {"value": tot_e / el, "ms_per_step": 1000 * el / args.steps,
+                                       "h2d_bytes_per_step": hb, "d2h_bytes_per_step": db, "total": tot_e,
+                                       "seconds": el}
     best = max(e2e_paths, key=lambda k: e2e_paths[k]["value"])
     e_total, e2e_s = e2e_paths[best]["total"], e2e_paths[best]["seconds"]
     h2d, d2h = e2e_paths[best]["h2d_bytes_per_step"], e2e_paths[best]["d2h_bytes_per_step"]

@@ -168,7 +168,9 @@ struct fm_server {
         }
         if (!batch && group[0]->mode == FM_MODE_TABLE) {
             const Request* r = group[0];
-            uint64_t trows = table_rows_override ? table_rows_override : r->table_rows;
+            // the caller's buffer bounds the rows that can be returned: a
+            // table of that size never needs a second run
+            uint64_t trows = table_rows_override ? table_rows_override : r->host_rows ? r->host_cap : r->table_rows;
             if (r->host_rows) trows = std::min<uint64_t>(trows, r->host_cap);
             trows = std::max<uint64_t>(trows, 1);
             uint64_t tb = trows * 4ull * r->query.p.q;
