@@ -361,7 +361,7 @@ def run_ours(args, rank, world, local):
             for t, qi in zip(tickets, qinfo):
                 r = srv.poll(t)
                 if r.status != fm.FM_OK:
-                    raise RuntimeError("served request failed with status %d" % r.status)
+                    raise RuntimeError("served request failed with status %d: %s" % (r.status, r.error.decode()))
                 c += r.count
                 d2h += r.rows_copied * qi.q * 4
                 srv.release(t)

@@ -97,7 +97,7 @@ class ServeResult(ctypes.Structure):
     _fields_ = [("done", ctypes.c_int32), ("status", ctypes.c_int32), ("count", ctypes.c_uint64),
                 ("rows_copied", ctypes.c_uint64), ("truncated", ctypes.c_int32), ("batch", ctypes.c_uint32),
                 ("lease_bytes", ctypes.c_uint64), ("attempts", ctypes.c_uint32), ("queue_ms", ctypes.c_double),
-                ("service_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+                ("service_ms", ctypes.c_double), ("latency_ms", ctypes.c_double), ("error", ctypes.c_char * 128)]
 
 
 class ServerStats(ctypes.Structure):

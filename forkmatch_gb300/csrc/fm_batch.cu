@@ -428,10 +428,8 @@ cudaError_t launch_batch_level(const BatchParams& p, bool roots, int grid, int h
 int batch_blocks_per_sm(bool roots, size_t smem) {
     void* f = roots ? (void*)&k_bexpand<true> : (void*)&k_bexpand<false>;
     void* fh = roots ? (void*)&k_bexpand_heavy<true> : (void*)&k_bexpand_heavy<false>;
-    if (smem > 48 * 1024) {
-        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(fh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    }
+    allow_dynamic_smem(f);
+    allow_dynamic_smem(fh);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, kBWarps * 32, smem) != cudaSuccess || n < 1) n = 1;
     return n;

@@ -173,6 +173,9 @@ struct ExpandParams {
 cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups, int grid, int heavy_grid,
                           int block, size_t smem, cudaStream_t s);
 size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps);
+// Let kernel f launch with up to the device's opt-in shared memory (once per
+// device; safe from several host threads).
+void allow_dynamic_smem(const void* f);
 int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block);
 
 // The parts of a context other translation units use (fm_host.cu owns it).

@@ -36,6 +36,10 @@
 // `stop`, and exits; the host drains the output level (depth first) and
 // relaunches this level on the deferred chunks plus the unclaimed remainder.
 // Nothing spins and nothing traps.
+#include <mutex>
+#include <set>
+#include <utility>
+
 #include "fm_device.cuh"
 
 namespace fm {
@@ -488,12 +492,24 @@ size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps) {
     return (size_t)warps * per_warp_bytes(depth, nreq);
 }
 
+void allow_dynamic_smem(const void* f) {
+    // Raised once per (device, kernel) to the opt-in maximum: a per-launch
+    // value would race between host threads launching with different sizes.
+    static std::mutex mu;
+    static std::set<std::pair<int, const void*>> done;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (!done.insert({dev, f}).second) return;
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (optin > 0) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+}
+
 int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block) {
     void* f = pick(mode, roots, dups, false);
-    if (smem > 48 * 1024) {
-        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(pick(mode, roots, dups, true), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    }
+    allow_dynamic_smem(f);
+    allow_dynamic_smem(pick(mode, roots, dups, true));
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, block, smem) != cudaSuccess || n < 1) n = 1;
     return n;

@@ -20,6 +20,7 @@
 //     one chunk is retried at twice the size.
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -224,6 +225,7 @@ struct fm_server {
             pending.pop_front();
             r->t_start = Clock::now();
             r->res.status = FM_ERR_POOL;
+            std::snprintf(r->res.error, sizeof(r->res.error), "the pool cannot hold this request's smallest lease");
             r->res.done = 1;
             r->res.latency_ms = r->res.queue_ms = ms_between(r->t_submit, r->t_start);
             completed++;
@@ -352,6 +354,9 @@ void fm_server::worker(size_t i) {
         if (group.size() == 1) run_single(slot, group[0], L, lk);
         else run_batch(slot, group, L);
         const Clock::time_point t1 = Clock::now();
+        for (Request* r : group) {
+            if (r->res.status != FM_OK) std::snprintf(r->res.error, sizeof(r->res.error), "%s", fm_last_error());
+        }
         lk.lock();
         if (L.bytes) pool.release(L.off, L.bytes);
         running -= group.size();

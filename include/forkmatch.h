@@ -287,6 +287,7 @@ typedef struct fm_serve_result {
     double queue_ms;            /* submit -> admitted */
     double service_ms;          /* admitted -> done */
     double latency_ms;          /* submit -> done */
+    char error[128];            /* message of a failed request ("" on success) */
 } fm_serve_result;
 typedef struct fm_server_stats {
     uint64_t submitted, completed, queued, running;
