@@ -503,7 +503,11 @@ void allow_dynamic_smem(const void* f) {
     if (!done.insert({dev, f}).second) return;
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (optin > 0) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, f) != cudaSuccess) return;
+    // static shared memory counts against the same opt-in limit
+    const int dyn = optin - (int)fa.sharedSizeBytes;
+    if (dyn > 0) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
 }
 
 int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block) {
