@@ -504,10 +504,14 @@ void allow_dynamic_smem(const void* f) {
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, f) != cudaSuccess) return;
+    if (cudaFuncGetAttributes(&fa, f) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
     // static shared memory counts against the same opt-in limit
     const int dyn = optin - (int)fa.sharedSizeBytes;
-    if (dyn > 0) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    if (dyn > 0 && cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
+        cudaGetLastError();   // the launch reports a size it cannot take
 }
 
 int expand_blocks_per_sm(int mode, bool roots, bool dups, size_t smem, int block) {
