@@ -642,16 +642,8 @@ def run_serving(args, rank, world, local):
             continue
         text = qq.to_g_text()
         q = fm.Query.from_text(text)
-        ok = True
-        for frac in (4096, 256):
-            r = fm.match(ctx, g, q, mode=fm.MODE_COUNT, roots=(0, V // frac))
-            if r.count * frac > (1 << 26):
-                ok = False
-                break
-        if not ok:
-            continue
-        r = fm.match(ctx, g, q, mode=fm.MODE_COUNT)
-        if r.count > (1 << 27) or r.device_ms > 50.0:
+        r = fm.match(ctx, g, q, mode=fm.MODE_COUNT, work_limit=1 << 27, allow_limit=True)
+        if r.status != fm.FM_OK or r.device_ms > 50.0:
             continue
         queries.append(q)
         texts.append(text)
@@ -703,8 +695,8 @@ def run_serving(args, rank, world, local):
             "config": {"workload": "serving", "graph": "R-MAT(0.57,0.19,0.19,0.05) 2^%d vertices, %dM undirected "
                        "edges, 64 edge labels, 8 vertex labels uniform" % (scale, m // 1000000),
                        "queries": len(queries), "query_vertices": "%d-%d" % (min(sizes), max(sizes)),
-                       "screening": "walk-induced subgraphs; kept when a 1/4096 and a 1/256 root sample extrapolate "
-                                    "to <= 2^26 embeddings and the plain count is <= 2^27 within 50 ms",
+                       "screening": "walk-induced subgraphs; kept when the plain count finishes within a work "
+                                    "limit of 2^27 embeddings / partial matches and 50 ms",
                        "pool_gb": args.pool_gb, "slots": args.slots, "max_batch": args.max_batch,
                        "arrivals": "Poisson, %g s or %d requests per rate" % (args.serving_seconds,
                                                                              args.serving_requests)},

@@ -17,6 +17,7 @@ MAXQ = 32
 
 FM_OK = 0
 FM_ERR_OUTPUT_OVERFLOW = 12
+FM_ERR_LIMIT = 16
 MODE_TABLE, MODE_COUNT = 0, 1
 COLUMNS_REFERENCE, COLUMNS_QUERY_ID = 0, 1
 ORDER_AUTO, ORDER_REFERENCE = 0, 1
@@ -25,7 +26,7 @@ STATUS_NAMES = {
     0: "FM_OK", 1: "FM_ERR_ARG", 2: "FM_ERR_IO", 3: "FM_ERR_DATA_HEADER0", 4: "FM_ERR_DATA_TRAILER",
     5: "FM_ERR_DATA_HEADER", 6: "FM_ERR_DATA_LINE", 7: "FM_ERR_QUERY_FORMAT", 8: "FM_ERR_QUERY_MISSING",
     9: "FM_ERR_DISCONNECTED", 10: "FM_ERR_UNSUPPORTED", 11: "FM_ERR_POOL", 12: "FM_ERR_OUTPUT_OVERFLOW",
-    13: "FM_ERR_CUDA", 14: "FM_ERR_DEVICE", 15: "FM_ERR_NOMEM",
+    13: "FM_ERR_CUDA", 14: "FM_ERR_DEVICE", 15: "FM_ERR_NOMEM", 16: "FM_ERR_LIMIT",
 }
 
 # Every function include/forkmatch.h declares (checked by the CPU test suite).
@@ -67,7 +68,7 @@ class MatchOpts(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("columns", ctypes.c_int32), ("stream", ctypes.c_void_p),
                 ("host_rows", ctypes.c_void_p), ("host_rows_cap", ctypes.c_uint64),
                 ("root_begin", ctypes.c_uint32), ("root_end", ctypes.c_uint32), ("profile", ctypes.c_int32),
-                ("order", ctypes.c_int32), ("host_direct", ctypes.c_int32)]
+                ("order", ctypes.c_int32), ("host_direct", ctypes.c_int32), ("work_limit", ctypes.c_uint64)]
 
 
 class LevelStats(ctypes.Structure):
@@ -90,7 +91,7 @@ class BatchStats(ctypes.Structure):
 
 class ServerOpts(ctypes.Structure):
     _fields_ = [("slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32), ("min_lease_bytes", ctypes.c_uint64),
-                ("max_lease_bytes", ctypes.c_uint64)]
+                ("max_lease_bytes", ctypes.c_uint64), ("work_limit", ctypes.c_uint64)]
 
 
 class ServeResult(ctypes.Structure):
@@ -307,11 +308,14 @@ class PinnedRows:
 
 
 def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_rows=None, roots=None,
-          profile=False, stream=None, allow_truncation=False, order=ORDER_AUTO, host_direct=False):
+          profile=False, stream=None, allow_truncation=False, order=ORDER_AUTO, host_direct=False, work_limit=0,
+          allow_limit=False):
     """Run fm_match.  Returns the Result struct; with ``host_rows`` (a
     PinnedRows or a C-contiguous uint32 numpy array) the table is copied there.
     ``host_direct`` (PinnedRows only): the kernels write the table straight
-    into the pinned host buffer instead of device memory."""
+    into the pinned host buffer instead of device memory.  ``work_limit``:
+    stop after that many embeddings or partial matches (FM_ERR_LIMIT, raised
+    unless ``allow_limit``)."""
     o = MatchOpts()
     lib().fm_match_opts_default(ctypes.byref(o))
     o.mode = mode
@@ -319,6 +323,7 @@ def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_ro
     o.profile = 1 if profile else 0
     o.order = order
     o.host_direct = 1 if host_direct else 0
+    o.work_limit = int(work_limit)
     if stream is not None:
         o.stream = stream
     if roots is not None:
@@ -332,7 +337,9 @@ def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_ro
             o.host_rows_cap = host_rows.size // max(1, query.q)
     r = Result()
     st = lib().fm_match(ctx._h, graph._h, query._h, ctypes.byref(o), ctypes.byref(r))
-    _check(st, "fm_match", allow=(FM_ERR_OUTPUT_OVERFLOW,) if allow_truncation else ())
+    allow = ((FM_ERR_OUTPUT_OVERFLOW,) if allow_truncation else ()) + ((FM_ERR_LIMIT,) if allow_limit else ())
+    _check(st, "fm_match", allow=allow)
+    r.status = st
     return r
 
 
@@ -396,9 +403,9 @@ class Server:
     footprint against the context's slab, slots overlapping on the device,
     count-mode requests batched at the head of the queue."""
 
-    def __init__(self, ctx, graph, slots=4, max_batch=1, min_lease_bytes=0, max_lease_bytes=0):
+    def __init__(self, ctx, graph, slots=4, max_batch=1, min_lease_bytes=0, max_lease_bytes=0, work_limit=0):
         self.ctx, self.graph = ctx, graph
-        o = ServerOpts(slots, max_batch, min_lease_bytes, max_lease_bytes)
+        o = ServerOpts(slots, max_batch, min_lease_bytes, max_lease_bytes, work_limit)
         h = ctypes.c_void_p()
         _check(lib().fm_server_create(ctx._h, graph._h, ctypes.byref(o), ctypes.byref(h)), "fm_server_create")
         self._h = h

@@ -105,6 +105,7 @@ const char* fm_status_string(fm_status s) {
         case FM_ERR_CUDA: return "CUDA error";
         case FM_ERR_DEVICE: return "device status error";
         case FM_ERR_NOMEM: return "out of memory";
+        case FM_ERR_LIMIT: return "work limit reached";
     }
     return "unknown";
 }
@@ -381,6 +382,14 @@ struct MatchRun {
     bool profile;
     size_t prof_used = 0;
     int block = 256;
+    uint64_t work_limit = 0;         // partial matches produced, checked between launches
+
+    bool over_limit() const {
+        if (!work_limit) return false;
+        uint64_t s = 0;
+        for (uint32_t d = 1; d + 1 < plan->q; d++) s += res->level[d].produced;
+        return s > work_limit;
+    }
 
     int mode_of(uint32_t d) const {
         return (d == plan->q - 1) ? (table ? kModeLastTable : kModeLastCount) : kModeMid;
@@ -465,6 +474,7 @@ struct MatchRun {
                 return FM_ERR_DEVICE;
             }
         }
+        if (over_limit()) return FM_ERR_LIMIT;
         LaunchCtl snap[kMaxQ];
         std::memcpy(snap, ctx->h_ctl, q * sizeof(LaunchCtl));
         for (uint32_t d = q - 1; d >= 1; d--) {
@@ -531,6 +541,7 @@ struct MatchRun {
                 set_error("deferred-chunk list overflow");
                 return FM_ERR_DEVICE;
             }
+            if (over_limit()) return FM_ERR_LIMIT;
             const uint64_t claimed = std::min<uint64_t>(c.claim, items);
             const uint64_t fresh_claimed = claimed > ndef_in ? claimed - ndef_in : 0;
             const uint64_t carry = ndef_in > claimed ? ndef_in - claimed : 0;
@@ -662,6 +673,7 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
 
     FM_CUDA(cudaMemsetAsync(ctx->tot, 0, sizeof(MatchTotals), s));
     FM_CUDA(cudaEventRecord(ctx->ev0, s));
+    bool limited = false;
     if (q == 1) {
         uint64_t n = re - rb;
         if (table && n) {
@@ -724,8 +736,11 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         b.tot = ctx->tot;
         b.heavy = ctx->heavy;
         b.heavy_cap = ctx->heavy_cap;
+        b.work_limit = opts.work_limit;
+        run.work_limit = opts.work_limit;
         fm_status st = run.run(n_roots);
-        if (st != FM_OK) return st;
+        if (st == FM_ERR_LIMIT) limited = true;
+        else if (st != FM_OK) return st;
     }
     FM_CUDA(cudaEventRecord(ctx->ev1, s));
     FM_CUDA(cudaMemcpyAsync(ctx->h_tot, ctx->tot, sizeof(MatchTotals), cudaMemcpyDeviceToHost, s));
@@ -748,6 +763,10 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     }
     out->h2d_bytes = out->launches * sizeof(ExpandParams);
     out->d2h_bytes = out->launches * sizeof(LaunchCtl) + sizeof(MatchTotals) + out->rows_copied * q * 4;
+    if (limited || (ctx->h_tot->error & kLimitFlag)) {
+        set_error("work limit reached; count and rows are a lower bound");
+        return FM_ERR_LIMIT;
+    }
     if (out->truncated) {
         set_error("embedding table truncated at OUTPUT_PREALLOC; count is exact");
         return FM_ERR_OUTPUT_OVERFLOW;

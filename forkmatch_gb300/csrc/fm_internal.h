@@ -166,7 +166,11 @@ struct ExpandParams {
     HeavyEntry* heavy;
     uint32_t heavy_cap;             // entries; chunks are published only while room remains
     uint32_t max_warps;             // warps of the heavy pass (bounds concurrent publishers)
+    // last level: stop once the count (or reserved table rows) exceeds this,
+    // setting bit kLimitFlag in tot->error; 0 = no limit
+    unsigned long long work_limit;
 };
+constexpr unsigned int kLimitFlag = 2u;
 
 // Launch one level expansion: the main pass, then the heavy-chunk pass
 // (fm_match.cu).

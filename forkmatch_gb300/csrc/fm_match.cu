@@ -312,6 +312,33 @@ __device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpM
     }
 }
 
+// Work limit of a last level (warp-uniform result): lane 0 adds the warp's
+// recent count to the total, compares the total (or the table rows reserved)
+// with the limit and raises the limit flag.  Checked once per chunk or piece,
+// so a warp overshoots by at most one chunk's work.
+template <int MODE>
+__device__ __forceinline__ bool over_limit(const ExpandParams& P, uint32_t lane, unsigned long long n_count,
+                                           unsigned long long& n_flushed) {
+    int over = 0;
+    if (lane == 0) {
+        unsigned long long seen;
+        if (MODE == kModeLastCount) {
+            seen = *(volatile unsigned long long*)&P.tot->count;
+            if (n_count - n_flushed >= 4096) {
+                seen = atomicAdd(&P.tot->count, n_count - n_flushed) + (n_count - n_flushed);
+                n_flushed = n_count;
+            }
+        } else {
+            seen = *(volatile unsigned long long*)&P.tot->table_pos;
+        }
+        if (seen > P.work_limit) {
+            over = 1;
+            atomicOr(&P.tot->error, kLimitFlag);
+        }
+    }
+    return __shfl_sync(kFull, over, 0) != 0;
+}
+
 // Main pass: warps claim batches of chunks; long candidate ranges are
 // published to the heavy list instead of being walked by one warp.
 template <int MODE, bool ROOTS, bool DUPS>
@@ -328,6 +355,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
     const Tune T = make_tune(P, true);
 
     unsigned long long n_count = 0, n_lookups = 0, n_words = 0, n_parents = 0;
+    unsigned long long n_flushed = 0;  // part of n_count already added to tot->count (lane 0)
     unsigned long long credit = 0;   // level budget held by this warp (lane 0)
     uint32_t nst = 0;
     bool done = false;
@@ -340,6 +368,10 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
             first + T.claim_batch < T.n_items ? first + T.claim_batch : T.n_items;
         for (unsigned long long item = first; item < last; item++) {
             const uint32_t chunk = item_chunk(P, item);
+            if (MODE != kModeMid && P.work_limit && over_limit<MODE>(P, lane, n_count, n_flushed)) {
+                done = true;
+                break;
+            }
             if (MODE == kModeMid) {
                 // one lane reads the flag and broadcasts it, so the warp never splits
                 int stop = 0;
@@ -420,7 +452,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
             atomicAdd(&P.ctl->lookups, n_lookups);
             atomicAdd(&P.ctl->list_words, n_words);
         }
-        if (MODE == kModeLastCount && n_count) atomicAdd(&P.tot->count, n_count);
+        if (MODE == kModeLastCount && n_count > n_flushed) atomicAdd(&P.tot->count, n_count - n_flushed);
     }
 }
 
@@ -443,9 +475,10 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand_heavy(const __grid_co
     const uint32_t rb = P.plan.req_begin[d];
     const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k);
     const Tune T = make_tune(P, false);
-    unsigned long long n_count = 0;
+    unsigned long long n_count = 0, n_flushed = 0;
     uint32_t nst = 0;
     for (;;) {
+        if (MODE != kModeMid && P.work_limit && over_limit<MODE>(P, lane, n_count, n_flushed)) break;
         unsigned long long gp = 0;
         if (lane == 0) gp = atomicAdd(&P.ctl->claim2, 1ull);
         gp = __shfl_sync(kFull, gp, 0);
@@ -465,7 +498,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand_heavy(const __grid_co
         process_slots<MODE, ROOTS, DUPS>(P, m, e.chunk, begin, end, lane, d, k, col_depth_s, nst, n_count);
     }
     if (MODE != kModeLastCount && nst) flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s);
-    if (MODE == kModeLastCount && lane == 0 && n_count) atomicAdd(&P.tot->count, n_count);
+    if (MODE == kModeLastCount && lane == 0 && n_count > n_flushed) atomicAdd(&P.tot->count, n_count - n_flushed);
 }
 
 template <int MODE, bool ROOTS, bool DUPS>

@@ -146,7 +146,7 @@ struct fm_server {
     std::deque<Request*> pending;
     std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
     uint64_t next_ticket = 1;
-    uint64_t submitted = 0, completed = 0, running = 0, batches = 0, embeddings = 0;
+    uint64_t submitted = 0, completed = 0, running = 0, batches = 0, embeddings = 0, limited = 0;
     bool stop = false;
 
     // Lease for a group of requests (one request, or count-mode requests
@@ -196,7 +196,7 @@ struct fm_server {
     int admit_head(std::vector<Request*>& group, Lease& L) {
         group.clear();
         group.push_back(pending.front());
-        if (opts.max_batch > 1 && group[0]->mode == FM_MODE_COUNT) {
+        if (opts.max_batch > 1 && !opts.work_limit && group[0]->mode == FM_MODE_COUNT) {
             for (size_t i = 1; i < pending.size() && group.size() < opts.max_batch; i++) {
                 if (pending[i]->mode != FM_MODE_COUNT) break;
                 group.push_back(pending[i]);
@@ -262,6 +262,7 @@ void fm_server::run_single(Slot& slot, Request* r, Lease& L, std::unique_lock<st
         o.mode = r->mode;
         o.host_rows = r->host_rows;
         o.host_rows_cap = r->host_cap;
+        o.work_limit = opts.work_limit;
         st = fm_match(slot.ctx, graph, &r->query, &o, &res);
         r->res.attempts = attempt;
         r->res.lease_bytes = L.bytes;
@@ -367,6 +368,7 @@ void fm_server::worker(size_t i) {
             r->res.done = 1;
             completed++;
             if (r->res.status == FM_OK || r->res.status == FM_ERR_OUTPUT_OVERFLOW) embeddings += r->res.count;
+            if (r->res.status == FM_ERR_LIMIT) limited++;
         }
         cv_done.notify_all();
         cv_work.notify_all();

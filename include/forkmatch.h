@@ -49,7 +49,8 @@ typedef enum fm_status {
     FM_ERR_OUTPUT_OVERFLOW = 12,/* table truncated at OUTPUT_PREALLOC (count stays exact) */
     FM_ERR_CUDA = 13,           /* CUDA runtime error (fm_last_error() has the text) */
     FM_ERR_DEVICE = 14,         /* device-side status word reported an error */
-    FM_ERR_NOMEM = 15           /* allocation failed */
+    FM_ERR_NOMEM = 15,          /* allocation failed */
+    FM_ERR_LIMIT = 16           /* fm_match_opts.work_limit reached (count is a lower bound) */
 } fm_status;
 
 const char* fm_status_string(fm_status s);
@@ -162,6 +163,9 @@ typedef struct fm_match_opts {
     int32_t host_direct;        /* 1: the kernels write the table straight into host_rows over
                                    the host link (host_rows must be pinned, e.g. fm_host_alloc);
                                    no device copy of the table is kept */
+    uint64_t work_limit;        /* 0: none.  Otherwise stop once more than this many embeddings
+                                   were counted, or partial matches produced, and return
+                                   FM_ERR_LIMIT (count and rows are then a lower bound) */
 } fm_match_opts;
 
 /* Matching order.  Results (count, row set, column layout) do not depend on
@@ -274,6 +278,8 @@ typedef struct fm_server_opts {
     uint32_t max_batch;         /* count-mode requests matched together; 0 or 1 = one at a time */
     uint64_t min_lease_bytes;   /* smallest level-buffer lease; 0 = 256 MiB */
     uint64_t max_lease_bytes;   /* largest lease of one request; 0 = a quarter of the pool */
+    uint64_t work_limit;        /* per request (fm_match_opts.work_limit); 0 = none.  With a
+                                   limit, requests are not batched */
 } fm_server_opts;
 typedef struct fm_serve_result {
     int32_t done;               /* 0 = queued or running */

@@ -137,6 +137,32 @@ def test_heavy_chunks_split_across_warps(ctx):
     assert fm.match(ctx, g, fm.Query.from_text(p3), mode=fm.MODE_COUNT).count == 2 * n * (n - 1) + n * 2
 
 
+def test_work_limit_stops_early_with_a_lower_bound(ctx):
+    """K_{2,n}: 8 * C(n, 2) four-cycles.  A work limit far below stops the last
+    level (count mode and table mode) and the middle levels (host check), and
+    reports FM_ERR_LIMIT with a count between the limit and the full count."""
+    n = 3000
+    a = np.repeat(np.array([0, 1], dtype=np.uint32), n)
+    b = np.tile(np.arange(2, n + 2, dtype=np.uint32), 2)
+    src, dst = np.concatenate([a, b]), np.concatenate([b, a])
+    lab = np.ones(len(src), dtype=np.uint32)
+    g = fm.Graph.from_edges(ctx, n + 2, 2, src, dst, lab)
+    c4 = fm.Query.from_text(S.query_cycle(4, [1] * 4).to_g_text())
+    full = 8 * math.comb(n, 2)
+    assert fm.match(ctx, g, c4, mode=fm.MODE_COUNT, work_limit=full + 1).count == full
+    for mode in (fm.MODE_COUNT, fm.MODE_TABLE):
+        r = fm.match(ctx, g, c4, mode=mode, work_limit=1 << 20, allow_limit=True)
+        assert r.status == fm.FM_ERR_LIMIT
+        assert (1 << 20) < r.count < full
+    with pytest.raises(fm.FMError):
+        fm.match(ctx, g, c4, mode=fm.MODE_COUNT, work_limit=1 << 20)
+    # partial matches: a 5-path has 2 * n * (n - 1) * ... middle rows
+    p5 = fm.Query.from_text(S.query_path(5, [1] * 4).to_g_text())
+    r = fm.match(ctx, g, p5, mode=fm.MODE_COUNT, work_limit=1000, allow_limit=True)
+    assert r.status == fm.FM_ERR_LIMIT
+    g.close()
+
+
 def test_label_mismatch_and_absent_label(ctx):
     V, s, d, l = complete_graph(6, label=2)
     g = fm.Graph.from_edges(ctx, V, 3, s, d, l)

@@ -177,6 +177,28 @@ def test_pool_admits_only_what_fits(env):
         ctx.close()
 
 
+def test_request_work_limit(env):
+    big = int(np.argmax(env["want"]))
+    q, c = env["queries"][big], env["want"][big]
+    assert c > 1000
+    srv = fm.Server(env["ctx"], env["g"], slots=2, max_batch=8, work_limit=1000)
+    try:
+        t = srv.submit(q)
+        r = srv.poll(t)
+        assert r.status == fm.FM_ERR_LIMIT and r.batch == 1 and r.error
+        srv.release(t)
+    finally:
+        srv.close()
+    # a limit no request reaches: exact counts, and no batching under a limit
+    srv = fm.Server(env["ctx"], env["g"], slots=2, max_batch=8, work_limit=1 << 40)
+    try:
+        res = _run_all(srv, env["queries"])
+        assert [r.count for r in res] == env["want"]
+        assert max(r.batch for r in res) == 1
+    finally:
+        srv.close()
+
+
 def test_server_owns_the_slab(env):
     ctx, g, q = env["ctx"], env["g"], env["queries"][3]
     srv = fm.Server(ctx, g, slots=1)
