@@ -51,7 +51,8 @@ class GraphInfo(ctypes.Structure):
     _fields_ = [("vertices", ctypes.c_uint32), ("label_slots", ctypes.c_uint32), ("edges", ctypes.c_uint64),
                 ("segments", ctypes.c_uint64), ("long_segments", ctypes.c_uint64), ("nbr_words", ctypes.c_uint64),
                 ("max_list", ctypes.c_uint32), ("has_duplicates", ctypes.c_int32), ("device_bytes", ctypes.c_uint64),
-                ("build_ms", ctypes.c_double)]
+                ("build_ms", ctypes.c_double), ("bitmaps", ctypes.c_uint32), ("bitmap_min_len", ctypes.c_uint32),
+                ("bitmap_bytes", ctypes.c_uint64)]
 
 
 _U32Q = ctypes.c_uint32 * MAXQ

@@ -40,6 +40,8 @@ struct BatchParams {
     uint32_t nq;
     const uint4* seg;
     const uint32_t* nbr;
+    const uint32_t* bm;                       // list bitmaps (see DeviceGraph)
+    uint32_t bm_words;
     uint32_t V;
     // parents: columns 0..d-1, query id in column d (null at depth 1: roots)
     const uint32_t* pin;
@@ -258,7 +260,7 @@ __device__ __forceinline__ void bprocess(const BatchParams& P, const BMem& m, ui
             const uint32_t k = m.k_s[j];
             for (uint32_t i = 0; i < k && ok; i++) {
                 if (i == dj) continue;
-                ok = seg_has(m.segs_s[i * 32 + j], x, 1, P.nbr);
+                ok = seg_has(m.segs_s[i * 32 + j], x, 1, P.nbr, P.bm, P.bm_words);
             }
         }
         const bool fin = ok && m.fin_s[j];
@@ -842,6 +844,8 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
         run.base.nq = nq;
         run.base.seg = g.seg;
         run.base.nbr = g.nbr;
+        run.base.bm = g.bitmaps;
+        run.base.bm_words = g.bm_words;
         run.base.V = g.V;
         uint32_t longest = 1;
         for (const BatchPlan& bp : b->h_plans) longest = std::max(longest, bp.n_roots);

@@ -31,13 +31,20 @@ __device__ __forceinline__ uint32_t lower_bound_g(const uint32_t* __restrict__ a
     return lo;
 }
 
-// Does the list hold at least `need` copies of x?
-__device__ __forceinline__ bool seg_has(const uint4& s, uint32_t x, uint32_t need, const uint32_t* __restrict__ nbr) {
+// Does the list hold at least `need` copies of x?  Lists with a bitmap
+// (graphs without duplicate e-lines only, so need == 1) answer with one load.
+__device__ __forceinline__ bool seg_has(const uint4& s, uint32_t x, uint32_t need, const uint32_t* __restrict__ nbr,
+                                        const uint32_t* __restrict__ bm, uint32_t bm_words) {
     if (s.x <= 3) {
         const uint32_t c = (s.x > 0 && s.y == x) + (s.x > 1 && s.z == x) + (s.x > 2 && s.w == x);
         return c >= need;
     }
-    if (x < s.z || x > s.w) return false;
+    if (x > s.w) return false;
+    if (s.z & kBitmapMark) {
+        const uint32_t* b = bm + (uint64_t)(s.z & ~kBitmapMark) * bm_words;
+        return (__ldg(b + (x >> 5)) >> (x & 31)) & 1u;
+    }
+    if (x < s.z) return false;
     const uint32_t* a = nbr + (uint64_t)s.y * 4;
     const uint32_t pos = lower_bound_g(a, s.x, x) + need - 1;
     return pos < s.x && __ldg(a + pos) == x;

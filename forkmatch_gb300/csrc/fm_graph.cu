@@ -8,6 +8,8 @@
 // vectorised load; lists of up to 3 neighbours live inside the record (no
 // second access), longer lists start on a 16-byte boundary in `nbr`.
 // Sorting uses CUB's radix sort (graph build is not on the matching path).
+#include <cstdlib>
+
 #include <cub/cub.cuh>
 
 #include "fm_internal.h"
@@ -117,6 +119,50 @@ __global__ void k_seg_heads(const uint64_t* __restrict__ keys, const uint64_t* _
     }
 }
 
+// Lists of at least 2^min_log2 entries, counted by floor(log2(length)).
+__global__ void k_len_hist(const uint64_t* __restrict__ seg_start, uint64_t nseg, uint64_t E, uint32_t min_log2,
+                           unsigned int* __restrict__ hist) {
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < nseg; s += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t n = ((s + 1 < nseg) ? seg_start[s + 1] : E) - seg_start[s];
+        if (n >> min_log2) atomicAdd(hist + (63 - __clzll((long long)n)), 1u);
+    }
+}
+
+// Give every list of at least `thresh` entries a bitmap index (marked in the
+// z field of its record) and remember where its entries live.
+__global__ void k_bm_assign(const uint64_t* __restrict__ keys, const uint64_t* __restrict__ seg_start,
+                            const uint64_t* __restrict__ off16, uint64_t nseg, uint64_t E, uint32_t V, uint32_t vbits,
+                            uint64_t thresh, uint32_t cap, unsigned int* __restrict__ counter, uint4* __restrict__ seg,
+                            uint2* __restrict__ bm_list) {
+    const uint64_t vmask = (1ull << vbits) - 1;
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < nseg; s += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t b = seg_start[s];
+        const uint64_t n = ((s + 1 < nseg) ? seg_start[s + 1] : E) - b;
+        if (n < thresh || n <= 3) continue;
+        const unsigned int idx = atomicAdd(counter, 1u);
+        if (idx >= cap) continue;
+        const uint64_t k = keys[b];
+        const uint32_t src = (uint32_t)((k >> vbits) & vmask);
+        const uint32_t lab = (uint32_t)(k >> (2 * vbits));
+        reinterpret_cast<uint32_t*>(seg + (uint64_t)lab * V + src)[2] = kBitmapMark | idx;
+        bm_list[idx] = make_uint2((uint32_t)off16[s], (uint32_t)n);
+    }
+}
+
+// One block per bitmap: set the bit of every entry.
+__global__ void k_bm_fill(const uint32_t* __restrict__ nbr, const uint2* __restrict__ bm_list, uint32_t n_bm,
+                          uint32_t bm_words, uint32_t* __restrict__ bitmaps) {
+    for (uint32_t i = blockIdx.x; i < n_bm; i += gridDim.x) {
+        const uint2 e = bm_list[i];
+        const uint32_t* list = nbr + (uint64_t)e.x * 4;
+        uint32_t* bits = bitmaps + (uint64_t)i * bm_words;
+        for (uint32_t t = threadIdx.x; t < e.y; t += blockDim.x) {
+            const uint32_t x = list[t];
+            atomicOr(bits + (x >> 5), 1u << (x & 31));
+        }
+    }
+}
+
 uint32_t bits_for(uint64_t x) {   // bits needed to store values 0..x
     uint32_t b = 1;
     while (b < 64 && (x >> b)) ++b;
@@ -128,6 +174,23 @@ struct DevBuf {
     ~DevBuf() { if (p) cudaFree(p); }
     template <class T> T* as() { return (T*)p; }
 };
+
+uint64_t env_bytes(const char* name, uint64_t dflt) {
+    const char* v = std::getenv(name);
+    if (!v || !*v) return dflt;
+    char* end = nullptr;
+    const unsigned long long x = std::strtoull(v, &end, 10);
+    return (end && *end == 0) ? (uint64_t)x : dflt;
+}
+
+// Out-of-line (long) list count so far (device counter), read back.
+uint64_t nlong_hint(const unsigned long long* d_nlong, cudaStream_t s) {
+    unsigned long long n = 0;
+    if (cudaMemcpyAsync(&n, d_nlong, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return 1;
+    return n;
+}
 
 int grid_for(uint64_t n, int sms) {
     uint64_t b = (n + 255) / 256;
@@ -202,8 +265,9 @@ fm_status build_device_graph(DeviceGraph& g, uint32_t V, uint32_t L, uint64_t E,
         DevBuf temp2;
         FM_CUDA(cudaMalloc(&temp2.p, tb2));
         FM_CUDA(cub::DeviceScan::InclusiveSum(temp2.p, tb2, head.as<uint32_t>(), incl.as<uint32_t>(), (int64_t)E, s));
-        uint32_t nseg32 = 0;
+        uint32_t nseg32 = 0, dup_seen = 0;
         FM_CUDA(cudaMemcpyAsync(&nseg32, incl.as<uint32_t>() + (E - 1), 4, cudaMemcpyDeviceToHost, s));
+        FM_CUDA(cudaMemcpyAsync(&dup_seen, d_dup, 4, cudaMemcpyDeviceToHost, s));
         FM_CUDA(cudaStreamSynchronize(s));
         nseg = nseg32;
         DevBuf seg_start, len16, off16;
@@ -248,6 +312,56 @@ fm_status build_device_graph(DeviceGraph& g, uint32_t V, uint32_t L, uint64_t E,
         FM_CUDA(cudaStreamSynchronize(s));
         g.head_off.assign(L + 1, 0);
         for (uint32_t l = 0; l < L; l++) g.head_off[l + 1] = g.head_off[l] + cnt[l];
+
+        // membership bitmaps for the longest lists (not with duplicates: a
+        // bit cannot count copies; vertex ids must leave bit 31 of z free)
+        const uint64_t budget = env_bytes("FM_BITMAP_BYTES", 2ull << 30);
+        const uint64_t min_len = std::max<uint64_t>(4, env_bytes("FM_BITMAP_MIN_LEN", 64));
+        const uint32_t words = (V + 31) / 32;
+        const uint64_t cap64 = budget / (4ull * words);
+        if (!dup_seen && V < kBitmapMark && cap64 > 0 && nlong_hint(d_nlong, s) > 0) {
+            uint32_t min_log2 = 0;
+            while ((1ull << min_log2) < min_len) min_log2++;
+            DevBuf hist;
+            FM_CUDA(cudaMalloc(&hist.p, 64 * 4 + 4));
+            FM_CUDA(cudaMemsetAsync(hist.p, 0, 64 * 4 + 4, s));
+            k_len_hist<<<grid_for(nseg, sms), 256, 0, s>>>(seg_start.as<uint64_t>(), nseg, E, min_log2,
+                                                          hist.as<unsigned int>());
+            FM_CUDA(cudaGetLastError());
+            unsigned int h[64];
+            FM_CUDA(cudaMemcpyAsync(h, hist.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+            FM_CUDA(cudaStreamSynchronize(s));
+            const uint32_t cap = (uint32_t)std::min<uint64_t>(cap64, 1u << 30);
+            // smallest power-of-two threshold whose lists all fit the budget
+            uint64_t above = 0;
+            int pick = -1;
+            for (int b = 63; b >= (int)min_log2; b--) {
+                if (above + h[b] > cap) break;
+                above += h[b];
+                if (h[b]) pick = b;
+            }
+            if (pick >= 0 && above > 0) {
+                const uint64_t thresh = 1ull << pick;
+                uint64_t n_bm = 0;
+                for (int b = pick; b < 64; b++) n_bm += h[b];
+                DevBuf bm_list;
+                FM_CUDA(cudaMalloc(&bm_list.p, n_bm * sizeof(uint2)));
+                FM_CUDA(cudaMalloc(&g.bitmaps, n_bm * words * 4ull));
+                FM_CUDA(cudaMemsetAsync(g.bitmaps, 0, n_bm * words * 4ull, s));
+                unsigned int* counter = hist.as<unsigned int>() + 64;
+                k_bm_assign<<<grid_for(nseg, sms), 256, 0, s>>>(sorted, seg_start.as<uint64_t>(), off16.as<uint64_t>(),
+                                                               nseg, E, V, vbits, thresh, (uint32_t)n_bm, counter,
+                                                               g.seg, bm_list.as<uint2>());
+                FM_CUDA(cudaGetLastError());
+                const uint32_t fill_grid = (uint32_t)std::min<uint64_t>(n_bm, (uint64_t)sms * 16);
+                k_bm_fill<<<fill_grid, 256, 0, s>>>(g.nbr, bm_list.as<uint2>(), (uint32_t)n_bm, words, g.bitmaps);
+                FM_CUDA(cudaGetLastError());
+                FM_CUDA(cudaStreamSynchronize(s));
+                g.n_bitmaps = (uint32_t)n_bm;
+                g.bm_words = words;
+                g.bm_min_len = (uint32_t)thresh;
+            }
+        }
     } else {
         FM_CUDA(cudaMalloc(&g.nbr, 16));
         FM_CUDA(cudaMalloc(&g.heads, 16));

@@ -213,6 +213,8 @@ static void free_device_graph(DeviceGraph& g) {
     if (g.seg) cudaFree(g.seg);
     if (g.nbr) cudaFree(g.nbr);
     if (g.heads) cudaFree(g.heads);
+    if (g.bitmaps) cudaFree(g.bitmaps);
+    g.bitmaps = nullptr;
     g.seg = nullptr;
     g.nbr = nullptr;
     g.heads = nullptr;
@@ -308,7 +310,10 @@ fm_status fm_graph_get_info(const fm_graph* g, fm_graph_info* info) {
     info->nbr_words = d.nbr_words;
     info->max_list = d.max_len;
     info->has_duplicates = d.has_dups;
-    info->device_bytes = (uint64_t)d.L * d.V * 16 + d.nbr_words * 4 + d.segments * 4;
+    info->bitmaps = d.n_bitmaps;
+    info->bitmap_min_len = d.bm_min_len;
+    info->bitmap_bytes = (uint64_t)d.n_bitmaps * d.bm_words * 4;
+    info->device_bytes = (uint64_t)d.L * d.V * 16 + d.nbr_words * 4 + d.segments * 4 + info->bitmap_bytes;
     info->build_ms = d.build_ms;
     return FM_OK;
 }
@@ -712,6 +717,8 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         ExpandParams& b = run.base;
         b.seg = g.seg;
         b.nbr = g.nbr;
+        b.bm = g.bitmaps;
+        b.bm_words = g.bm_words;
         b.V = g.V;
         b.root_begin = rb;
         // Over the full vertex range the roots are the vertices that have an

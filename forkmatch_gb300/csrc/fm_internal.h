@@ -13,6 +13,7 @@ namespace fm {
 
 constexpr int kMaxQ = FM_MAX_QUERY_VERTICES;
 constexpr int kMaxReqTotal = 512;       // back edges over all depths of one query
+constexpr uint32_t kBitmapMark = 0x80000000u;   // long record: z holds a bitmap index
 constexpr uint32_t kNoVertex = 0xffffffffu;
 
 // Thread-local error text (fm_last_error).
@@ -47,6 +48,13 @@ struct DeviceGraph {
     // ascending.  A matching's roots come from the list of a depth-1 label.
     uint32_t* heads = nullptr;
     std::vector<uint64_t> head_off;      // L + 1 entries (host)
+    // Membership bitmaps of the longest lists: a long record whose z field
+    // has kBitmapMark set keeps its bitmap (bm_words u32 over all vertices) at
+    // bitmaps + (z & ~kBitmapMark) * bm_words instead of its minimum.
+    uint32_t* bitmaps = nullptr;
+    uint32_t bm_words = 0;
+    uint32_t n_bitmaps = 0;
+    uint32_t bm_min_len = 0;
     uint64_t nbr_words = 0;
     uint64_t segments = 0, long_segments = 0;
     uint32_t max_len = 0;
@@ -136,6 +144,8 @@ struct ExpandParams {
     // graph
     const uint4* seg;
     const uint32_t* nbr;
+    const uint32_t* bm;             // list bitmaps (see DeviceGraph)
+    uint32_t bm_words;
     uint32_t V;
     // parents
     const uint32_t* pin;            // SoA: column c at pin + c*pstride (null for roots)

@@ -124,7 +124,7 @@ __device__ __forceinline__ bool slot_check(const ExpandParams& P, uint32_t x, ui
     if (DUPS) need = seg_rank(ds, t, x, P.nbr) + 1;
     for (uint32_t i = 0; i < k && ok; i++) {
         if (i == dj) continue;
-        ok = seg_has(segs_s[i * 32 + j], x, need, P.nbr);
+        ok = seg_has(segs_s[i * 32 + j], x, need, P.nbr, P.bm, P.bm_words);
     }
     return ok;
 }

@@ -239,6 +239,8 @@ extern "C" fm_status fm_match_static(const fm_graph* graph, const fm_query* quer
     ExpandParams& b = run.base;
     b.seg = g.seg;
     b.nbr = g.nbr;
+    b.bm = g.bitmaps;
+    b.bm_words = g.bm_words;
     b.V = g.V;
     b.root_begin = 0;
     b.table = rows_out;

@@ -87,7 +87,11 @@ void* fm_context_stream(fm_context* ctx);
  * in device memory.  Replaces parseGraph/parseCSR/csrToTrie and
  * BaseGPUGraph::neighbours (src/trie.cuh:1051-1222, 800-951, 750-795, 266-310).
  * Graph memory is sized to fit at load time (not carved from the slab), so one
- * resident graph serves every context on the same device. */
+ * resident graph serves every context on the same device.  The longest lists
+ * also get a bitmap over all vertices (membership in one load instead of a
+ * binary search) while the bitmaps fit FM_BITMAP_BYTES (environment, default
+ * 2 GiB; 0 disables) and are at least FM_BITMAP_MIN_LEN (default 64) long;
+ * graphs with duplicate e-lines get none. */
 typedef struct fm_graph fm_graph;
 typedef struct fm_graph_info {
     uint32_t vertices;
@@ -100,6 +104,9 @@ typedef struct fm_graph_info {
     int32_t has_duplicates;     /* some (label, src, dst) e-line occurs twice */
     uint64_t device_bytes;      /* graph bytes resident on the device */
     double build_ms;            /* device build time */
+    uint32_t bitmaps;           /* lists that also have a membership bitmap over all vertices */
+    uint32_t bitmap_min_len;    /* shortest list given a bitmap (0: none) */
+    uint64_t bitmap_bytes;
 } fm_graph_info;
 
 /* `.g` file / in-memory text (the reference parser's grammar, README.md:5-27). */

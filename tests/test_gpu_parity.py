@@ -137,6 +137,42 @@ def test_heavy_chunks_split_across_warps(ctx):
     assert fm.match(ctx, g, fm.Query.from_text(p3), mode=fm.MODE_COUNT).count == 2 * n * (n - 1) + n * 2
 
 
+@pytest.mark.parametrize("min_len,budget", [("4", None), ("16", "4194304"), (None, "0")])
+def test_list_bitmaps_give_identical_results(ctx, monkeypatch, min_len, budget):
+    """Membership bitmaps for long lists (down to 4 entries, under a small
+    budget that covers only the longest, or none at all): counts, tables and
+    work counters equal the oracle's."""
+    if min_len is not None:
+        monkeypatch.setenv("FM_BITMAP_MIN_LEN", min_len)
+    if budget is not None:
+        monkeypatch.setenv("FM_BITMAP_BYTES", budget)
+    G = S.rmat(13, 50000, seed=41, n_elabels=3)
+    src, dst, lab = G.directed()
+    g = fm.Graph.from_edges(ctx, G.V, 4, src, dst, lab)
+    og = O.Graph.from_edges(G.V, 4, src, dst, lab)
+    info = g.info()
+    if budget == "0":
+        assert info.bitmaps == 0
+    else:
+        assert info.bitmaps > 0 and info.bitmap_min_len >= int(min_len)
+        assert info.bitmap_bytes <= (int(budget) if budget else 2 << 30)
+    rng = np.random.default_rng(42)
+    done = 0
+    for i in range(40):
+        k = int(rng.integers(3, 7))
+        q = S.query_random_walk(G, k, rng, tree=bool(i % 3 == 0), bias=1.0)
+        if q is None:
+            continue
+        try:
+            O.match(og, O.plan(q.to_g_text(), enumerate_aut=0), limit=1 << 21, scan_limit=1 << 25)
+        except O.OracleError:
+            continue
+        check_case(ctx, g, og, q.to_g_text(), table=True, max_rows=1 << 21)
+        done += 1
+    assert done >= 8
+    g.close()
+
+
 def test_work_limit_stops_early_with_a_lower_bound(ctx):
     """K_{2,n}: 8 * C(n, 2) four-cycles.  A work limit far below stops the last
     level (count mode and table mode) and the middle levels (host check), and
