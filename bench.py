@@ -458,7 +458,8 @@ def run_batched(args, rank, world, local):
     rec = [q["count"] for q in meta]
     table_words = sum(q["count"] * q["k"] for q in meta)
     out_bytes = ((table_words * 4 + (256 << 20)) >> 20) << 20
-    ctx = fm.Context(prealloc_bytes=24 * GB + out_bytes + (128 << 20), soln_prealloc_bytes=24 * GB,
+    # one shared level buffer per depth holds every query's partial matches
+    ctx = fm.Context(prealloc_bytes=128 * GB + out_bytes + (128 << 20), soln_prealloc_bytes=128 * GB,
                      output_prealloc_bytes=out_bytes, bank_rows=1 << 16, device=local)
     t = time.time()
     g = fm.Graph.from_edges(ctx, G.V, G.n_elabels + 1, src, dst, lab)
@@ -642,8 +643,8 @@ def run_serving(args, rank, world, local):
             continue
         text = qq.to_g_text()
         q = fm.Query.from_text(text)
-        r = fm.match(ctx, g, q, mode=fm.MODE_COUNT, work_limit=1 << 27, allow_limit=True)
-        if r.status != fm.FM_OK or r.device_ms > 50.0:
+        r = fm.match(ctx, g, q, mode=fm.MODE_COUNT, work_limit=1 << 25, allow_limit=True)
+        if r.status != fm.FM_OK or r.device_ms > 20.0:
             continue
         queries.append(q)
         texts.append(text)
@@ -696,7 +697,7 @@ def run_serving(args, rank, world, local):
                        "edges, 64 edge labels, 8 vertex labels uniform" % (scale, m // 1000000),
                        "queries": len(queries), "query_vertices": "%d-%d" % (min(sizes), max(sizes)),
                        "screening": "walk-induced subgraphs; kept when the plain count finishes within a work "
-                                    "limit of 2^27 embeddings / partial matches and 50 ms",
+                                    "limit of 2^25 embeddings / partial matches and 20 ms",
                        "pool_gb": args.pool_gb, "slots": args.slots, "max_batch": args.max_batch,
                        "arrivals": "Poisson, %g s or %d requests per rate" % (args.serving_seconds,
                                                                              args.serving_requests)},
