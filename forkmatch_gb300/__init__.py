@@ -37,7 +37,8 @@ EXPORTS = [
     "fm_match_opts_default", "fm_match", "fm_host_alloc", "fm_host_free", "fm_version", "fm_device_count",
     "fm_match_static", "fm_batch_create", "fm_batch_run", "fm_batch_rows", "fm_batch_copy_rows", "fm_batch_tune",
     "fm_batch_free", "fm_batch_copy_tables", "fm_server_create", "fm_server_submit", "fm_server_poll",
-    "fm_server_release", "fm_server_get_stats", "fm_server_destroy",
+    "fm_server_release", "fm_server_get_stats", "fm_server_destroy", "fm_graph_write_cache", "fm_table_write",
+    "fm_table_to_query_columns",
 ]
 
 
@@ -150,6 +151,9 @@ def lib():
         L.fm_batch_copy_tables.argtypes = [vp, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]
         L.fm_batch_tune.argtypes = [vp, ctypes.POINTER(BatchStats)]
         L.fm_batch_free.argtypes = [vp]
+        L.fm_graph_write_cache.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        L.fm_table_write.argtypes = [ctypes.c_char_p, vp, u64, u32, i32, i32]
+        L.fm_table_to_query_columns.argtypes = [vp, vp, u64, vp]
         L.fm_server_create.argtypes = [vp, vp, ctypes.POINTER(ServerOpts), ctypes.POINTER(vp)]
         L.fm_server_submit.argtypes = [vp, vp, i32, vp, u64, ctypes.POINTER(u64)]
         L.fm_server_poll.argtypes = [vp, u64, i32, ctypes.POINTER(ServeResult)]
@@ -450,6 +454,43 @@ class Server:
 
     def __del__(self):
         self.close()
+
+
+def write_graph_cache(text_path, cache_path):
+    """Parse a .g file once and store it as a binary graph cache, which
+    Graph.from_file (fm_graph_load_file) loads without parsing."""
+    _check(lib().fm_graph_write_cache(os.fsencode(text_path), os.fsencode(cache_path)), "fm_graph_write_cache")
+
+
+TABLE_HEADER = np.dtype([("magic", "S8"), ("q", "<u4"), ("columns", "<u4"), ("rows", "<u8"), ("sorted", "<u4"),
+                         ("reserved", "<u4")])
+
+
+def write_table(path, rows, columns=COLUMNS_REFERENCE, sort=True):
+    """fm_table_write: rows (n, q) uint32 in the layout ``columns``."""
+    rows = np.ascontiguousarray(rows, dtype=np.uint32)
+    n, q = rows.shape
+    _check(lib().fm_table_write(os.fsencode(path), rows.ctypes.data, n, q, columns, 1 if sort else 0),
+           "fm_table_write")
+
+
+def read_table(path):
+    """Returns (rows (n, q) uint32, header) of an embedding-table file."""
+    with open(path, "rb") as f:
+        h = np.frombuffer(f.read(TABLE_HEADER.itemsize), dtype=TABLE_HEADER)[0]
+        if h["magic"] != b"FMTB0001":
+            raise ValueError("not an embedding-table file")
+        rows = np.fromfile(f, dtype="<u4", count=int(h["rows"]) * int(h["q"]))
+    return rows.reshape(int(h["rows"]), int(h["q"])), h
+
+
+def to_query_columns(query, rows_ref):
+    """Reference column layout -> query-vertex-id layout."""
+    rows_ref = np.ascontiguousarray(rows_ref, dtype=np.uint32)
+    out = np.empty_like(rows_ref)
+    _check(lib().fm_table_to_query_columns(query._h, rows_ref.ctypes.data, rows_ref.shape[0], out.ctypes.data),
+           "fm_table_to_query_columns")
+    return out
 
 
 def match_static(graph, query, rows_device_ptr=None, rows_cap=0, stream=None, allow_truncation=False):

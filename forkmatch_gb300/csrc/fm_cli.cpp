@@ -9,8 +9,9 @@
 // data lines (where the reference traps on the device) return 79.
 //
 // Extras, all optional: FM_MODE=count (count only), FM_COLUMNS=query (table
-// columns by query vertex id), FM_OUTPUT=<file> (write the table as raw u32
-// rows), plus the FM_PREALLOC / FM_SOLN_PREALLOC / FM_OUTPUT_PREALLOC /
+// columns by query vertex id), FM_OUTPUT=<file> (write the table as an
+// embedding-table file, fm_table_write; FM_OUTPUT_SORTED=1 sorts the rows),
+// plus the FM_PREALLOC / FM_SOLN_PREALLOC / FM_OUTPUT_PREALLOC /
 // FM_CUR_BANK_SIZE knobs.
 #include <chrono>
 #include <cstdio>
@@ -116,18 +117,18 @@ int main(int argc, char** argv) {
 
     const char* outp = std::getenv("FM_OUTPUT");
     if (outp && *outp && opts.mode == FM_MODE_TABLE) {
+        // copy through the library so no CUDA call is needed here, then write
+        // an embedding-table file (FM_OUTPUT_SORTED=1: lexicographic rows)
         std::vector<uint32_t> rows(res.rows * res.q);
-        FILE* f = std::fopen(outp, "wb");
-        if (f) {
-            // copy through the library so no CUDA call is needed here
-            fm_match_opts o2 = opts;
-            o2.host_rows = rows.data();
-            o2.host_rows_cap = res.rows;
-            fm_result r2;
-            fm_match(ctx, graph, query, &o2, &r2);
-            std::fwrite(rows.data(), 4, (size_t)r2.rows_copied * r2.q, f);
-            std::fclose(f);
-        }
+        fm_match_opts o2 = opts;
+        o2.host_rows = rows.data();
+        o2.host_rows_cap = res.rows;
+        fm_result r2;
+        fm_match(ctx, graph, query, &o2, &r2);
+        const char* so = std::getenv("FM_OUTPUT_SORTED");
+        const int sorted = so && std::strcmp(so, "1") == 0;
+        if (fm_table_write(outp, rows.data(), r2.rows_copied, r2.q, opts.columns, sorted) != FM_OK)
+            std::fprintf(stderr, "warning: %s\n", fm_last_error());
     }
     fm_query_free(query);
     fm_graph_free(graph);

@@ -288,6 +288,57 @@ static bool read_file(const char* path, std::string& buf) {
     return true;
 }
 
+// Binary graph cache: the parsed e-lines of a .g file, so a large graph is
+// loaded without parsing text again.  Little-endian:
+//   "FMGB0001", u32 vertices, u32 label slots, u64 e-lines, u32 label bytes
+//   (1), u32 0, then src[E] u32, dst[E] u32, label[E] u8.
+namespace {
+const char kCacheMagic[8] = {'F', 'M', 'G', 'B', '0', '0', '0', '1'};
+struct CacheHeader {
+    char magic[8];
+    uint32_t V, L;
+    uint64_t E;
+    uint32_t lab_bytes, reserved;
+};
+static_assert(sizeof(CacheHeader) == 32, "cache header layout");
+}  // namespace
+
+fm_status fm_graph_write_cache(const char* text_path, const char* cache_path) {
+    if (!text_path || !cache_path) return FM_ERR_ARG;
+    std::string buf;
+    if (!read_file(text_path, buf)) {
+        set_error(std::string("missing file ") + text_path);
+        return FM_ERR_IO;
+    }
+    EdgeArrays ea;
+    fm_status st = parse_data_text(buf.data(), buf.size(), ea);
+    if (st != FM_OK) return st;
+    std::string().swap(buf);
+    CacheHeader h;
+    std::memcpy(h.magic, kCacheMagic, 8);
+    h.V = ea.V;
+    h.L = ea.L;
+    h.E = ea.src.size();
+    h.lab_bytes = 1;
+    h.reserved = 0;
+    std::vector<uint8_t> lab8(h.E);
+    for (uint64_t i = 0; i < h.E; i++) lab8[i] = (uint8_t)ea.lab[i];   // label slots <= 256
+    std::ofstream f(cache_path, std::ios::binary | std::ios::trunc);
+    if (!f) {
+        set_error(std::string("cannot write ") + cache_path);
+        return FM_ERR_IO;
+    }
+    f.write((const char*)&h, sizeof(h));
+    f.write((const char*)ea.src.data(), h.E * 4);
+    f.write((const char*)ea.dst.data(), h.E * 4);
+    f.write((const char*)lab8.data(), h.E);
+    if (!f) {
+        set_error(std::string("cannot write ") + cache_path);
+        return FM_ERR_IO;
+    }
+    return FM_OK;
+}
+
 fm_status fm_graph_load_file(fm_context* ctx, const char* path, fm_graph** out) {
     if (!ctx || !path || !out) return FM_ERR_ARG;
     *out = nullptr;
@@ -295,6 +346,23 @@ fm_status fm_graph_load_file(fm_context* ctx, const char* path, fm_graph** out) 
     if (!read_file(path, buf)) {
         set_error(std::string("missing file ") + path);
         return FM_ERR_IO;
+    }
+    if (buf.size() >= sizeof(CacheHeader) && std::memcmp(buf.data(), kCacheMagic, 8) == 0) {
+        CacheHeader h;
+        std::memcpy(&h, buf.data(), sizeof(h));
+        if (h.lab_bytes != 1 || h.L == 0 || h.L > FM_MAX_LABEL + 1 ||
+            buf.size() != sizeof(h) + h.E * 9) {
+            set_error("graph cache: bad header or size");
+            return FM_ERR_DATA_HEADER;
+        }
+        const char* p = buf.data() + sizeof(h);
+        std::vector<uint32_t> src(h.E), dst(h.E), lab(h.E);
+        std::memcpy(src.data(), p, h.E * 4);
+        std::memcpy(dst.data(), p + h.E * 4, h.E * 4);
+        const uint8_t* l8 = (const uint8_t*)(p + h.E * 8);
+        for (uint64_t i = 0; i < h.E; i++) lab[i] = l8[i];
+        std::string().swap(buf);
+        return graph_from_host_arrays(ctx, h.V, h.L, h.E, src.data(), dst.data(), lab.data(), out);
     }
     return fm_graph_load_text(ctx, buf.data(), buf.size(), out);
 }

@@ -109,8 +109,14 @@ typedef struct fm_graph_info {
     uint64_t bitmap_bytes;
 } fm_graph_info;
 
-/* `.g` file / in-memory text (the reference parser's grammar, README.md:5-27). */
+/* `.g` file / in-memory text (the reference parser's grammar, README.md:5-27).
+ * fm_graph_load_file also takes a binary graph cache (below) at the same path. */
 fm_status fm_graph_load_file(fm_context* ctx, const char* path, fm_graph** out);
+/* Parse a .g file once and store its e-lines as a binary graph cache
+ * ("FMGB0001" header: u32 vertices, u32 label slots, u64 e-lines, u32 label
+ * bytes = 1, u32 0; then src[E] u32, dst[E] u32, label[E] u8), which
+ * fm_graph_load_file reads without parsing.  Host only, no device. */
+fm_status fm_graph_write_cache(const char* text_path, const char* cache_path);
 fm_status fm_graph_load_text(fm_context* ctx, const char* text, uint64_t len, fm_graph** out);
 /* Directed e-lines from host arrays (both directions must be listed). */
 fm_status fm_graph_from_edges(fm_context* ctx, uint32_t vertices, uint32_t label_slots, uint64_t edges,
@@ -321,6 +327,19 @@ fm_status fm_server_release(fm_server* s, uint64_t ticket);
 fm_status fm_server_get_stats(fm_server* s, fm_server_stats* out);
 /* Finishes every queued request, then stops the slots and returns the slab. */
 void fm_server_destroy(fm_server* s);
+
+/* Embedding-table files.  The reference copies its table to the host and
+ * drops it (src/smsm.cu:1328-1348); these keep it for parity tooling.
+ * File: "FMTB0001", u32 q, u32 columns (fm_columns), u64 rows, u32 sorted,
+ * u32 0, then rows x q u32 (little-endian).  sort != 0 writes the rows in
+ * lexicographic order, so equal row sets give byte-identical files.  `rows`
+ * is host memory in the layout `columns` names. */
+fm_status fm_table_write(const char* path, const uint32_t* rows, uint64_t n, uint32_t q, int32_t columns,
+                         int32_t sort);
+/* Reference column layout -> query-vertex-id layout (column c = image of query
+ * vertex c); rows_out may not alias rows_ref. */
+fm_status fm_table_to_query_columns(const fm_query* query, const uint32_t* rows_ref, uint64_t n,
+                                    uint32_t* rows_out);
 
 /* Pinned host memory helpers (cudaHostAlloc / cudaFreeHost). */
 void* fm_host_alloc(uint64_t bytes);

@@ -4,6 +4,7 @@ Every test here runs the product kernels on the GPU and compares with the
 oracle (counts bit-exact, tables as sorted row sets, per-level work counters
 exact) or with closed-form counts.  Integer work: no tolerance anywhere."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -370,3 +371,45 @@ def test_data_parser_errors(ctx, text, status):
     with pytest.raises(fm.FMError) as ei:
         fm.Graph.from_text(ctx, text)
     assert ei.value.status == status
+
+
+def test_graph_cache_loads_the_same_graph(ctx, tmp_path):
+    G = S.rmat(12, 20000, seed=61, n_elabels=4)
+    p = tmp_path / "d.g"
+    p.write_bytes(G.to_g_text())
+    c = tmp_path / "d.fmgb"
+    fm.write_graph_cache(str(p), str(c))
+    a = fm.Graph.from_file(ctx, str(p))
+    b = fm.Graph.from_file(ctx, str(c))
+    ia, ib = a.info(), b.info()
+    for f in ("vertices", "label_slots", "edges", "segments", "long_segments", "max_list", "bitmaps"):
+        assert getattr(ia, f) == getattr(ib, f), f
+    for qq in (S.query_cycle(4, [1, 2, 3, 4]), S.query_path(5, [1, 1, 2, 3]), S.query_clique(4, [1, 2])):
+        q = fm.Query.from_text(qq.to_g_text())
+        ca, ra, _ = fm.match_table(ctx, a, q, max_rows=1 << 20)
+        cb, rb, _ = fm.match_table(ctx, b, q, max_rows=1 << 20)
+        assert ca == cb and np.array_equal(sorted_rows(ra), sorted_rows(rb))
+    a.close()
+    b.close()
+
+
+def test_cli_writes_sorted_table_file(ctx, tmp_path):
+    import subprocess
+    G = S.erdos_renyi(500, 2500, seed=71, n_elabels=2)
+    d = tmp_path / "d.g"
+    d.write_bytes(G.to_g_text())
+    qt = S.query_cycle(4, [1, 2, 1, 2]).to_g_text()
+    qf = tmp_path / "q.g"
+    qf.write_bytes(qt)
+    out = tmp_path / "t.fmtb"
+    env = dict(os.environ, FM_OUTPUT=str(out), FM_OUTPUT_SORTED="1", FM_PREALLOC=str(3 << 30),
+               FM_SOLN_PREALLOC=str(1 << 30), FM_OUTPUT_PREALLOC=str(1 << 30))
+    r = subprocess.run([os.path.join(os.path.dirname(fm.LIB_PATH), "ForkMatch"), str(qf), str(d)],
+                       capture_output=True, text=True, env=env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rows, h = fm.read_table(str(out))
+    src, dst, lab = G.directed()
+    og = O.Graph.from_edges(G.V, 3, src, dst, lab)
+    oc, orows, _ = O.match(og, O.plan(qt, enumerate_aut=0), table=True, table_cap=1 << 20)
+    assert h["sorted"] == 1 and h["rows"] == oc
+    assert np.array_equal(rows, sorted_rows(orows))

@@ -100,3 +100,51 @@ def test_cli_wrong_argument_count_exits_99():
     r = subprocess.run([fm.CLI_PATH], capture_output=True, text=True)
     assert r.returncode == 99
     assert r.stdout.startswith("Trie Graph Problem")
+
+
+def test_graph_cache_holds_the_parsed_e_lines(tmp_path):
+    """fm_graph_write_cache parses a .g file once; its e-lines equal the ones
+    in the text (the oracle's parser reads the same text)."""
+    from forkmatch_gb300 import synth as S
+    G = S.erdos_renyi(300, 900, seed=5, n_elabels=7)
+    text = G.to_g_text()
+    p = tmp_path / "data.g"
+    p.write_bytes(text)
+    c = tmp_path / "data.fmgb"
+    fm.write_graph_cache(str(p), str(c))
+    raw = c.read_bytes()
+    assert raw[:8] == b"FMGB0001"
+    import numpy as np
+    V, L = np.frombuffer(raw[8:16], dtype="<u4")
+    E = int(np.frombuffer(raw[16:24], dtype="<u8")[0])
+    src, dst, lab = G.directed()
+    assert (V, E) == (300, len(src)) and L == 8
+    body = raw[32:]
+    assert len(body) == 9 * E
+    cs = np.frombuffer(body[: 4 * E], dtype="<u4")
+    cd = np.frombuffer(body[4 * E: 8 * E], dtype="<u4")
+    cl = np.frombuffer(body[8 * E:], dtype=np.uint8)
+    got = sorted(zip(cs.tolist(), cd.tolist(), cl.tolist()))
+    assert got == sorted(zip(src.tolist(), dst.tolist(), lab.tolist()))
+    with pytest.raises(fm.FMError):
+        fm.write_graph_cache(str(tmp_path / "missing.g"), str(c))
+
+
+def test_table_files_sorted_and_in_query_columns(tmp_path):
+    import numpy as np
+    rng = np.random.default_rng(3)
+    rows = rng.integers(0, 50, size=(5000, 4)).astype(np.uint32)
+    p = tmp_path / "t.fmtb"
+    fm.write_table(str(p), rows, sort=True)
+    got, h = fm.read_table(str(p))
+    assert h["q"] == 4 and h["rows"] == 5000 and h["sorted"] == 1 and h["columns"] == fm.COLUMNS_REFERENCE
+    assert np.array_equal(got, rows[np.lexsort(rows.T[::-1])])
+    fm.write_table(str(p), rows, sort=False)
+    assert np.array_equal(fm.read_table(str(p))[0], rows)
+    # reference layout: column i = image of the vertex matched at depth q-1-i
+    from forkmatch_gb300 import synth as S
+    q = fm.Query.from_text(S.query_path(4, [1, 2, 3]).to_g_text())
+    info = q.info()
+    out = fm.to_query_columns(q, rows)
+    for i in range(4):
+        assert np.array_equal(out[:, info.order[4 - 1 - i]], rows[:, i])
