@@ -386,9 +386,12 @@ def test_graph_cache_loads_the_same_graph(ctx, tmp_path):
         assert getattr(ia, f) == getattr(ib, f), f
     for qq in (S.query_cycle(4, [1, 2, 3, 4]), S.query_path(5, [1, 1, 2, 3]), S.query_clique(4, [1, 2])):
         q = fm.Query.from_text(qq.to_g_text())
-        ca, ra, _ = fm.match_table(ctx, a, q, max_rows=1 << 20)
-        cb, rb, _ = fm.match_table(ctx, b, q, max_rows=1 << 20)
-        assert ca == cb and np.array_equal(sorted_rows(ra), sorted_rows(rb))
+        ca = fm.match(ctx, a, q, mode=fm.MODE_COUNT).count
+        assert fm.match(ctx, b, q, mode=fm.MODE_COUNT).count == ca
+        if ca <= 1 << 20:
+            _, ra, _ = fm.match_table(ctx, a, q, max_rows=1 << 20)
+            _, rb, _ = fm.match_table(ctx, b, q, max_rows=1 << 20)
+            assert np.array_equal(sorted_rows(ra), sorted_rows(rb))
     a.close()
     b.close()
 
