@@ -387,7 +387,6 @@ fm_status fm_server_create(fm_context* ctx, const fm_graph* g, const fm_server_o
     if (o.slots > 64) o.slots = 64;
     if (o.max_batch == 0) o.max_batch = 1;
     if (o.max_batch > 4096) o.max_batch = 4096;
-    if (o.min_lease_bytes == 0) o.min_lease_bytes = 256ull << 20;
     const ContextView cv = context_view(ctx);
     if (g->g.device != cv.device) {
         set_error("graph and context live on different devices");
@@ -414,6 +413,13 @@ fm_status fm_server_create(fm_context* ctx, const fm_graph* g, const fm_server_o
     s->base = slab;
     s->pool.init(pool_bytes);
     if (o.max_lease_bytes == 0) o.max_lease_bytes = std::max<uint64_t>(pool_bytes / 4, kGranule);
+    // The footprint model assumes independent e-lines and underestimates
+    // skewed graphs badly, and a level buffer that is too small costs a
+    // host-driven drain per refill; so by default every slot may hold half
+    // of its even share of the pool, whatever the estimate says.
+    if (o.min_lease_bytes == 0)
+        o.min_lease_bytes = std::max<uint64_t>(256ull << 20, pool_bytes / (2ull * o.slots) / kGranule * kGranule);
+    o.min_lease_bytes = std::min(o.min_lease_bytes, o.max_lease_bytes);
     s->opts = o;
     s->min_rows = (uint64_t)g->g.max_len * 32 + 32 + cv.bank_rows;
     for (uint32_t i = 0; i < o.slots; i++) {

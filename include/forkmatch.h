@@ -289,7 +289,7 @@ typedef struct fm_server fm_server;
 typedef struct fm_server_opts {
     uint32_t slots;             /* requests on the device at once; 0 = 4 */
     uint32_t max_batch;         /* count-mode requests matched together; 0 or 1 = one at a time */
-    uint64_t min_lease_bytes;   /* smallest level-buffer lease; 0 = 256 MiB */
+    uint64_t min_lease_bytes;   /* smallest level-buffer lease; 0 = pool / (2 * slots), at least 256 MiB */
     uint64_t max_lease_bytes;   /* largest lease of one request; 0 = a quarter of the pool */
     uint64_t work_limit;        /* per request (fm_match_opts.work_limit); 0 = none.  With a
                                    limit, requests are not batched */
