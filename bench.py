@@ -58,6 +58,7 @@ def parse_args():
     ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--max-batch", type=int, default=32)
     ap.add_argument("--pool-gb", type=int, default=120)
+    ap.add_argument("--skew-limit", type=int, default=1 << 36, help="work limit per query of the skew workload")
     return ap.parse_args()
 
 
@@ -715,6 +716,76 @@ def run_serving(args, rank, world, local):
     return 0
 
 
+def run_skew(args, rank, world, local):
+    """Skewed low-selectivity stress: count-only stars, 4-cycles and 4-cliques
+    on a Chung-Lu graph with hubs, every match bounded by a work limit; level
+    buffers kept small so that hub chunks defer and drain.  Bit-exactness is
+    checked on root samples the oracle finishes."""
+    import torch
+    import forkmatch_gb300 as fm
+    from forkmatch_gb300 import synth as S
+    from forkmatch_gb300 import workloads as W
+    from oracle import oracle as O
+    if world > 1:
+        raise SystemExit("--workload skew runs on one GPU")
+    torch.cuda.set_device(local)
+    t = time.time()
+    G = W.skew_graph()
+    src, dst, lab = G.directed()
+    gen_s = time.time() - t
+    ctx = fm.Context(prealloc_bytes=8 * GB, soln_prealloc_bytes=4 * GB, output_prealloc_bytes=1 * GB,
+                     bank_rows=1 << 20, device=local)
+    g = fm.Graph.from_edges(ctx, G.V, G.n_elabels + 1, src, dst, lab)
+    info = g.info()
+    og = O.Graph.from_edges(G.V, G.n_elabels + 1, src, dst, lab)
+    shapes = [("star5", S.query_star(5, [1, 1, 1, 1]), [1, 1, 1, 1]),
+              ("star5_mixed", S.query_star(5, [1, 1, 2, 2]), [1, 1, 2, 2]),
+              ("cycle4", S.query_cycle(4, [1, 1, 1, 1]), None), ("cycle4_mixed", S.query_cycle(4, [1, 2, 1, 2]), None),
+              ("clique4", S.query_clique(4, [1]), None), ("clique4_mixed", S.query_clique(4, [1, 2]), None)]
+    limit = args.skew_limit
+    out = []
+    tot_count = 0
+    tot_ms = 0.0
+    for name, qq, leaves in shapes:
+        text = qq.to_g_text()
+        q = fm.Query.from_text(text)
+        fm.match(ctx, g, q, mode=fm.MODE_COUNT, roots=(0, 1024))   # warm-up
+        r = fm.match(ctx, g, q, mode=fm.MODE_COUNT, work_limit=limit, allow_limit=True)
+        row = {"query": name, "status": "complete" if r.status == fm.FM_OK else "work limit reached",
+               "count": int(r.count), "device_ms": r.device_ms, "launches": int(r.launches),
+               "embeddings_per_s": r.count / (r.device_ms / 1000.0) if r.device_ms > 0 else None}
+        if leaves is not None:
+            row["closed_form_count"] = W.star_count_closed_form(G, leaves)
+        # bit-exact on root samples the oracle finishes (hub roots skipped)
+        p = O.plan(text, enumerate_aut=0)
+        checked = []
+        for start in range(0, G.V, 4096):
+            if len(checked) >= 3:
+                break
+            try:
+                oc = O.match(og, p, roots=(start, start + 64), limit=1 << 24, scan_limit=1 << 28)[0]
+            except O.OracleError:
+                continue
+            gc = fm.match(ctx, g, q, mode=fm.MODE_COUNT, roots=(start, start + 64)).count
+            checked.append({"roots": [start, start + 64], "oracle": int(oc), "gpu": int(gc)})
+        row["samples"] = checked
+        row["samples_bitexact"] = bool(checked) and all(c["oracle"] == c["gpu"] for c in checked)
+        out.append(row)
+        tot_count += r.count
+        tot_ms += r.device_ms
+    line = {"metric": METRIC, "value": tot_count / (tot_ms / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": 1,
+            "warmup": 1, "ms_per_step": tot_ms, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+            "dtype": "u64 counts", "data": "synthetic (seeded generators)",
+            "config": {"workload": "skew", "graph": "Chung-Lu 2^21 vertices, exponent 2.1, degree cap 2^20, 32M "
+                       "undirected edges, 1 vertex label, 2 edge labels", "max_list": info.max_list,
+                       "work_limit": limit, "soln_prealloc_gb": 4, "mode": "count only"},
+            "queries": out, "generate_s": gen_s}
+    print(json.dumps(line), flush=True)
+    g.close()
+    ctx.close()
+    return 0
+
+
 def verify_rows(ctx, g, queries, qinfo, edges, roots, sample=2048):
     """Size-independent check: sampled table rows are injective and every query
     e-line maps onto a data e-line with the same label."""
@@ -789,6 +860,8 @@ def main():
         return run_batched(args, rank, world, local)
     if args.workload == "serving":
         return run_serving(args, rank, world, local)
+    if args.workload == "skew":
+        return run_skew(args, rank, world, local)
     return run_ours(args, rank, world, local)
 
 

@@ -21,6 +21,11 @@ batched (the multi-query workload):
     query set with per-query counts is recorded in
     tests/golden/workload_batched.json.
 
+skew (the stress workload for level buffers and work splitting):
+    Chung-Lu, 2^21 vertices, power-law exponent 2.1, expected degrees capped
+    at 2^20, 32M distinct undirected edges, one vertex label, 2 edge labels;
+    5-vertex stars, 4-cycles and 4-cliques, count only (u64).
+
 serving (the request-loop workload):
     R-MAT(0.57, 0.19, 0.19, 0.05), 2^24 vertices, 256M distinct undirected
     edges (512M directed e-lines), vertex labels uniform over 8, edge labels
@@ -44,6 +49,7 @@ PLAIN_AT_SCALE = dict(scale=20, m=16_000_000, n_elabels=32, n_vlabels=4, seed=2,
 PLAIN_SMALL = dict(n=1000, m=2000, n_elabels=87, seed=1)
 BATCHED = dict(scale=22, m=64_000_000, n_elabels=64, n_vlabels=8, seed=5, vlabel_seed=6)
 SERVING = dict(scale=24, m=256_000_000, n_elabels=64, n_vlabels=8, seed=7, vlabel_seed=8)
+SKEW = dict(n=1 << 21, m=32_000_000, n_elabels=2, exponent=2.1, max_degree=1 << 20, seed=9)
 
 
 def edge_hash(src, dst, lab):
@@ -74,6 +80,28 @@ def serving_graph(scale=None, m=None):
     rng = np.random.default_rng(p["vlabel_seed"])
     vlab = rng.integers(0, p["n_vlabels"], size=1 << p["scale"], dtype=np.uint32)
     return S.rmat(p["scale"], p["m"], p["seed"], p["n_elabels"], vlab=vlab, n_vlabels=p["n_vlabels"])
+
+
+def skew_graph():
+    p = SKEW
+    return S.chung_lu(p["n"], p["m"], p["seed"], p["n_elabels"], exponent=p["exponent"], max_degree=p["max_degree"])
+
+
+def star_count_closed_form(G, leaf_labels):
+    """Embeddings of a star whose leaves carry `leaf_labels`: sum over centres
+    of the product, per label, of the falling factorial of the centre's
+    degree in that label (labels partition a vertex's neighbours).  Float:
+    the value can exceed 2^64."""
+    src, dst, lab = G.directed()
+    total = np.ones(G.V)
+    for l in sorted(set(leaf_labels)):
+        k = leaf_labels.count(l)
+        d = np.bincount(src[lab == l], minlength=G.V).astype(np.float64)
+        f = np.ones(G.V)
+        for i in range(k):
+            f *= np.maximum(d - i, 0)
+        total *= f
+    return float(total.sum())
 
 
 def plain_small_graph():

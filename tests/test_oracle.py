@@ -124,3 +124,18 @@ def test_data_parser_errors(text, code):
     with pytest.raises(O.OracleError) as ei:
         O.Graph.parse(text)
     assert ei.value.code == code
+
+
+def test_star_closed_form_equals_oracle_count():
+    """The skew workload reports star counts in closed form (a product of
+    falling factorials of per-label degrees at each centre); on a small
+    Chung-Lu graph it equals the oracle's enumeration."""
+    from forkmatch_gb300 import synth as S
+    from forkmatch_gb300 import workloads as W
+    G = S.chung_lu(2000, 4000, seed=9, n_elabels=2, max_degree=60)
+    src, dst, lab = G.directed()
+    og = O.Graph.from_edges(G.V, 3, src, dst, lab)
+    for leaves in ([1, 1, 1, 1], [1, 1, 2, 2], [1, 2], [2, 2, 2]):
+        q = S.query_star(len(leaves) + 1, leaves)
+        c = O.match(og, O.plan(q.to_g_text(), enumerate_aut=0))[0]
+        assert c == W.star_count_closed_form(G, leaves)
