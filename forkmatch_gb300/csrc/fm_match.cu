@@ -53,7 +53,7 @@ using dev::seg_has;
 using dev::slot_locate;
 
 constexpr int kWarps = 8;
-constexpr uint32_t kStage = 512;           // staged survivors per warp
+constexpr uint32_t kStage = 256;           // staged survivors per warp
 constexpr uint32_t kHeavyMaxPieces = 65536;
 
 // Rank of position t within its run of equal values.
@@ -342,7 +342,7 @@ __device__ __forceinline__ bool over_limit(const ExpandParams& P, uint32_t lane,
 // Main pass: warps claim batches of chunks; long candidate ranges are
 // published to the heavy list instead of being walked by one warp.
 template <int MODE, bool ROOTS, bool DUPS>
-__global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant__ ExpandParams P) {
+__global__ void __launch_bounds__(kWarps * 32, 6) k_expand(const __grid_constant__ ExpandParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint8_t col_depth_s[kMaxQ];
     if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P.plan.col_depth[threadIdx.x];
@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_expand(const __grid_constant
 // the published chunks, reloads that chunk and walks its piece of the slots.
 // The main pass already holds the chunk's output budget and counted its work.
 template <int MODE, bool ROOTS, bool DUPS>
-__global__ void __launch_bounds__(kWarps * 32, 4) k_expand_heavy(const __grid_constant__ ExpandParams P) {
+__global__ void __launch_bounds__(kWarps * 32, 6) k_expand_heavy(const __grid_constant__ ExpandParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint8_t col_depth_s[kMaxQ];
     if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P.plan.col_depth[threadIdx.x];
