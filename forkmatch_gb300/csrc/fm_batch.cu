@@ -183,6 +183,7 @@ __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem
             }
         }
         n = best;
+        if (k > 2) drv = dev::order_lists(m.segs_s, lane, k, drv);
     }
     k_out = k;
     uint32_t incl = n;

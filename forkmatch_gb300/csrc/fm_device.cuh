@@ -50,6 +50,28 @@ __device__ __forceinline__ bool seg_has(const uint4& s, uint32_t x, uint32_t nee
     return pos < s.x && __ldg(a + pos) == x;
 }
 
+// Reorder one parent's records (column `lane` of recs): the driver first, the
+// other lists shortest first, so a candidate meets the most selective
+// membership test first and most rejections take one test.  Returns the
+// driver's new index (0).  Membership does not depend on the order.
+__device__ __forceinline__ uint32_t order_lists(uint4* recs, uint32_t lane, uint32_t k, uint32_t drv) {
+    if (drv != 0) {
+        const uint4 t = recs[lane];
+        recs[lane] = recs[drv * 32 + lane];
+        recs[drv * 32 + lane] = t;
+    }
+    for (uint32_t i = 2; i < k; i++) {
+        const uint4 key = recs[i * 32 + lane];
+        uint32_t j = i;
+        while (j > 1 && recs[(j - 1) * 32 + lane].x > key.x) {
+            recs[j * 32 + lane] = recs[(j - 1) * 32 + lane];
+            j--;
+        }
+        recs[j * 32 + lane] = key;
+    }
+    return 0;
+}
+
 // Slot s of a chunk belongs to parent j (the last j with excl[j] <= s), at
 // position t of that parent's driver list.
 __device__ __forceinline__ void slot_locate(uint32_t s, const uint32_t* excl_s, uint32_t& j, uint32_t& t) {

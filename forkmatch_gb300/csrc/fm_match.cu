@@ -243,6 +243,7 @@ __device__ __forceinline__ uint32_t load_chunk(const ExpandParams& P, const Warp
             }
         }
         n = best;
+        if (k > 2) drv = dev::order_lists(m.segs_s, lane, k, drv);
     }
     uint32_t incl = n;
 #pragma unroll
