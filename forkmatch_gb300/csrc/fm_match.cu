@@ -54,6 +54,7 @@ using dev::slot_locate;
 
 constexpr int kWarps = 8;
 constexpr uint32_t kStage = 256;           // staged survivors per warp
+constexpr uint32_t kSlots = 2;             // candidate slots per lane per round
 constexpr uint32_t kHeavyMaxPieces = 65536;
 
 // Rank of position t within its run of equal values.
@@ -257,54 +258,53 @@ __device__ __forceinline__ uint32_t load_chunk(const ExpandParams& P, const Warp
     return __shfl_sync(kFull, incl, 31);
 }
 
-// Evaluate slots [begin, end) of the loaded chunk: two slots per lane per round
-// with both driver loads in flight; survivors go to the stage, which is
-// flushed whenever it cannot take another round.
+// Evaluate slots [begin, end) of the loaded chunk: kSlots slots per lane per
+// round with all their driver loads in flight; survivors go to the stage,
+// which is flushed whenever it cannot take another round.
 template <int MODE, bool ROOTS, bool DUPS>
 __device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpMem& m, uint32_t chunk,
                                               uint32_t begin, uint32_t end, uint32_t lane, uint32_t d, uint32_t k,
                                               const uint8_t* col_depth_s, uint32_t& nst,
                                               unsigned long long& n_count) {
     const uint32_t pbase = chunk * 32;
-    for (uint32_t base = begin; base < end; base += 64) {
-        const uint32_t s0 = base + lane, s1 = base + 32 + lane;
-        const bool a0 = s0 < end, a1 = s1 < end;
-        uint32_t j0 = 0, t0 = 0, j1 = 0, t1 = 0, x0 = 0, x1 = 0, dj0 = 0, dj1 = 0;
-        uint4 ds0 = make_uint4(0, 0, 0, 0), ds1 = make_uint4(0, 0, 0, 0);
-        if (a0) {
-            slot_locate(s0, m.excl_s, j0, t0);
-            dj0 = m.drv_s[j0];
-            ds0 = m.segs_s[dj0 * 32 + j0];
-            x0 = seg_at(ds0, t0, P.nbr);
+    for (uint32_t base = begin; base < end; base += 32 * kSlots) {
+        uint32_t j[kSlots], t[kSlots], x[kSlots];
+        bool ok[kSlots];
+        // every driver load of the round is issued before any check
+#pragma unroll
+        for (uint32_t u = 0; u < kSlots; u++) {
+            const uint32_t s = base + 32 * u + lane;
+            j[u] = t[u] = x[u] = 0;
+            ok[u] = s < end;
+            if (ok[u]) {
+                slot_locate(s, m.excl_s, j[u], t[u]);
+                x[u] = seg_at(m.segs_s[m.drv_s[j[u]] * 32 + j[u]], t[u], P.nbr);
+            }
         }
-        if (a1) {
-            slot_locate(s1, m.excl_s, j1, t1);
-            dj1 = m.drv_s[j1];
-            ds1 = m.segs_s[dj1 * 32 + j1];
-            x1 = seg_at(ds1, t1, P.nbr);
-        }
-        const bool ok0 = a0 && slot_check<DUPS>(P, x0, t0, j0, dj0, ds0, m.segs_s, m.rows_s, k, d);
-        const bool ok1 = a1 && slot_check<DUPS>(P, x1, t1, j1, dj1, ds1, m.segs_s, m.rows_s, k, d);
-        const unsigned b0 = __ballot_sync(kFull, ok0);
-        const unsigned b1 = __ballot_sync(kFull, ok1);
-        if (MODE == kModeLastCount) {
-            n_count += __popc(b0) + __popc(b1);
-            continue;
+#pragma unroll
+        for (uint32_t u = 0; u < kSlots; u++) {
+            if (ok[u]) {
+                const uint32_t dj = m.drv_s[j[u]];
+                ok[u] = slot_check<DUPS>(P, x[u], t[u], j[u], dj, m.segs_s[dj * 32 + j[u]], m.segs_s, m.rows_s, k, d);
+            }
         }
         const unsigned lt = (1u << lane) - 1u;
-        if (ok0) {
-            const uint32_t q0 = nst + __popc(b0 & lt);
-            m.stp[q0] = pbase + j0;
-            m.stx[q0] = x0;
+#pragma unroll
+        for (uint32_t u = 0; u < kSlots; u++) {
+            const unsigned b = __ballot_sync(kFull, ok[u]);
+            if (MODE == kModeLastCount) {
+                n_count += __popc(b);
+                continue;
+            }
+            if (ok[u]) {
+                const uint32_t q = nst + __popc(b & lt);
+                m.stp[q] = pbase + j[u];
+                m.stx[q] = x[u];
+            }
+            nst += __popc(b);
         }
-        nst += __popc(b0);
-        if (ok1) {
-            const uint32_t q1 = nst + __popc(b1 & lt);
-            m.stp[q1] = pbase + j1;
-            m.stx[q1] = x1;
-        }
-        nst += __popc(b1);
-        if (nst > kStage - 64) {
+        if (MODE == kModeLastCount) continue;
+        if (nst > kStage - 32 * kSlots) {
             __syncwarp();
             flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s);
             nst = 0;
