@@ -163,11 +163,21 @@ __device__ __forceinline__ uint32_t parent_col(const ExpandParams& P, uint32_t c
     return __ldg(P.pin + c * P.pstride + p);
 }
 
+// Column c of staged parent p: from the warp's copy of chunk `cur` in shared
+// memory when p belongs to it (most survivors do), else from the level.
+template <bool ROOTS>
+__device__ __forceinline__ uint32_t staged_col(const ExpandParams& P, const WarpMem& m, uint32_t c, uint32_t p,
+                                               uint32_t cur) {
+    if ((p >> 5) == cur) return m.rows_s[c * 32 + (p & 31)];
+    return parent_col<ROOTS>(P, c, p);
+}
+
 // Write the staged survivors with one atomic: column by column into the next
-// level (SoA), or row-major into the table; every store is coalesced.
+// level (SoA), or row-major into the table; every store is coalesced.  `cur`
+// is the chunk whose rows the warp holds in shared memory.
 template <int MODE, bool ROOTS>
 __device__ __forceinline__ void flush_stage(const ExpandParams& P, const WarpMem& m, uint32_t nst, uint32_t lane,
-                                            uint32_t d, const uint8_t* col_depth_s) {
+                                            uint32_t d, const uint8_t* col_depth_s, uint32_t cur) {
     unsigned long long pos0 = 0;
     if (lane == 0)
         pos0 = atomicAdd(MODE == kModeMid ? &P.ctl->produced : &P.tot->table_pos, (unsigned long long)nst);
@@ -175,7 +185,7 @@ __device__ __forceinline__ void flush_stage(const ExpandParams& P, const WarpMem
     if (MODE == kModeMid) {
         for (uint32_t c = 0; c < d; c++) {
             uint32_t* col = P.pout + c * P.ocap + pos0;
-            for (uint32_t i = lane; i < nst; i += 32) col[i] = parent_col<ROOTS>(P, c, m.stp[i]);
+            for (uint32_t i = lane; i < nst; i += 32) col[i] = staged_col<ROOTS>(P, m, c, m.stp[i], cur);
         }
         uint32_t* col = P.pout + d * P.ocap + pos0;
         for (uint32_t i = lane; i < nst; i += 32) col[i] = m.stx[i];
@@ -194,19 +204,19 @@ __device__ __forceinline__ void flush_stage(const ExpandParams& P, const WarpMem
                 for (uint32_t c = 0; c < q; c += 4) {
                     uint4 v;
                     uint32_t dep = col_depth_s[c];
-                    v.x = dep < d ? parent_col<ROOTS>(P, dep, p) : x;
+                    v.x = dep < d ? staged_col<ROOTS>(P, m, dep, p, cur) : x;
                     dep = col_depth_s[c + 1];
-                    v.y = dep < d ? parent_col<ROOTS>(P, dep, p) : x;
+                    v.y = dep < d ? staged_col<ROOTS>(P, m, dep, p, cur) : x;
                     dep = col_depth_s[c + 2];
-                    v.z = dep < d ? parent_col<ROOTS>(P, dep, p) : x;
+                    v.z = dep < d ? staged_col<ROOTS>(P, m, dep, p, cur) : x;
                     dep = col_depth_s[c + 3];
-                    v.w = dep < d ? parent_col<ROOTS>(P, dep, p) : x;
+                    v.w = dep < d ? staged_col<ROOTS>(P, m, dep, p, cur) : x;
                     *(uint4*)(o + c) = v;
                 }
             } else {
                 for (uint32_t c = 0; c < q; c++) {
                     const uint32_t dep = col_depth_s[c];
-                    o[c] = dep < d ? parent_col<ROOTS>(P, dep, p) : x;
+                    o[c] = dep < d ? staged_col<ROOTS>(P, m, dep, p, cur) : x;
                 }
             }
         }
@@ -306,7 +316,7 @@ __device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpM
         if (MODE == kModeLastCount) continue;
         if (nst > kStage - 32 * kSlots) {
             __syncwarp();
-            flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s);
+            flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s, chunk);
             nst = 0;
         }
         __syncwarp();
@@ -357,6 +367,7 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_expand(const __grid_constant
 
     unsigned long long n_count = 0, n_lookups = 0, n_words = 0, n_parents = 0;
     unsigned long long n_flushed = 0;  // part of n_count already added to tot->count (lane 0)
+    uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
     unsigned long long credit = 0;   // level budget held by this warp (lane 0)
     uint32_t nst = 0;
     bool done = false;
@@ -388,6 +399,7 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_expand(const __grid_constant
             bool valid;
             unsigned long long w;
             const uint32_t total = load_chunk<ROOTS>(P, m, chunk, lane, d, k, rb, T.n_parents, valid, w);
+            last_chunk = chunk;
             if (MODE == kModeMid && total) {
                 int ok = 1;
                 if (lane == 0) {
@@ -440,7 +452,7 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_expand(const __grid_constant
             process_slots<MODE, ROOTS, DUPS>(P, m, chunk, 0, total, lane, d, k, col_depth_s, nst, n_count);
         }
     }
-    if (MODE != kModeLastCount && nst) flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s);
+    if (MODE != kModeLastCount && nst) flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s, last_chunk);
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
         n_lookups += __shfl_down_sync(kFull, n_lookups, o);
@@ -477,6 +489,7 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_expand_heavy(const __grid_co
     const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k);
     const Tune T = make_tune(P, false);
     unsigned long long n_count = 0, n_flushed = 0;
+    uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
     uint32_t nst = 0;
     for (;;) {
         if (MODE != kModeMid && P.work_limit && over_limit<MODE>(P, lane, n_count, n_flushed)) break;
@@ -496,9 +509,10 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_expand_heavy(const __grid_co
         bool valid;
         unsigned long long w;
         load_chunk<ROOTS>(P, m, e.chunk, lane, d, k, rb, T.n_parents, valid, w);
+        last_chunk = e.chunk;
         process_slots<MODE, ROOTS, DUPS>(P, m, e.chunk, begin, end, lane, d, k, col_depth_s, nst, n_count);
     }
-    if (MODE != kModeLastCount && nst) flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s);
+    if (MODE != kModeLastCount && nst) flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s, last_chunk);
     if (MODE == kModeLastCount && lane == 0 && n_count > n_flushed) atomicAdd(&P.tot->count, n_count - n_flushed);
 }
 
