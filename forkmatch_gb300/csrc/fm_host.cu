@@ -270,10 +270,15 @@ fm_status fm_graph_from_edges(fm_context* ctx, uint32_t vertices, uint32_t label
 fm_status fm_graph_load_text(fm_context* ctx, const char* text, uint64_t len, fm_graph** out) {
     if (!ctx || !out || (!text && len)) return FM_ERR_ARG;
     *out = nullptr;
-    EdgeArrays ea;
-    fm_status st = parse_data_text(text, len, ea);
-    if (st != FM_OK) return st;
-    return graph_from_host_arrays(ctx, ea.V, ea.L, ea.src.size(), ea.src.data(), ea.dst.data(), ea.lab.data(), out);
+    FM_CUDA(cudaSetDevice(ctx->device));
+    std::unique_ptr<fm_graph> g(new fm_graph());
+    fm_status st = parse_data_text_device(text, len, ctx->stream, g->g);
+    if (st != FM_OK) {
+        free_device_graph(g->g);
+        return st;
+    }
+    *out = g.release();
+    return FM_OK;
 }
 
 static bool read_file(const char* path, std::string& buf) {

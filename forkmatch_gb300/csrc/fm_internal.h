@@ -248,6 +248,9 @@ struct EdgeArrays {
     std::vector<uint32_t> src, dst, lab;
 };
 fm_status parse_data_text(const char* text, uint64_t len, EdgeArrays& out);
+// The same grammar and checks, parsed on the device straight into a graph
+// build (fm_ingest.cu).
+fm_status parse_data_text_device(const char* text, uint64_t len, cudaStream_t s, DeviceGraph& g);
 fm_status compile_query_text(const char* text, uint64_t len, Plan& out);
 
 }  // namespace fm

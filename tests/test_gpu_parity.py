@@ -416,3 +416,55 @@ def test_cli_writes_sorted_table_file(ctx, tmp_path):
     oc, orows, _ = O.match(og, O.plan(qt, enumerate_aut=0), table=True, table_cap=1 << 20)
     assert h["sorted"] == 1 and h["rows"] == oc
     assert np.array_equal(rows, sorted_rows(orows))
+
+
+def _host_parse_status(tmp_path, text):
+    p = tmp_path / "h.g"
+    p.write_bytes(text)
+    try:
+        fm.write_graph_cache(str(p), str(tmp_path / "h.fmgb"))
+    except fm.FMError as e:
+        return e.status, str(e)
+    return 0, ""
+
+
+def test_device_parser_agrees_with_host_parser(ctx, tmp_path):
+    """fm_graph_load_text parses on the device; fm_graph_write_cache parses on
+    the host.  Same status and message on malformed text, same graph and
+    counts on valid text (several blocks of 4 KiB, labels above 255 dropped)."""
+    head = b"t # 0\n3 4 1 2\nv 0 1\nv 1 1\nv 2 1\n"
+    bad = [
+        head + b"e 0 1 1\ne 1 0 1\ne 1 2 2\ne 2 1 2\nt # -1\n",
+        head + b"e 0 1 1\ne 1 0 1\ne 1 2 2\ne 2 1 2t # -1",
+        head + b"e 0 1 1\ne 1 0 1\ne 1 2 2\ne 2 1 2\ne 0 2 1\nt # -1",
+        head + b"e 0 1 1\n\ne 1 0 1\nt # -1",
+        head + b"e 0 1 1 \ne 1 0 1\nt # -1",
+        head + b"e 0 1 99999999999\nt # -1",
+        head + b"e 0 1 3\nt # -1",
+        head + b"v 3 1\nt # -1",
+        head + b"e 0 1 1\r\nt # -1",
+        head + b"e 0 1\nt # -1",
+        b"t # 0\n3 4 1 2\n",
+    ]
+    for text in bad:
+        hs, hm = _host_parse_status(tmp_path, text)
+        with pytest.raises(fm.FMError) as ei:
+            fm.Graph.from_text(ctx, text)
+        assert ei.value.status == hs, (text, hm, str(ei.value))
+        assert str(ei.value).split("(", 1)[1] == hm.split("(", 1)[1]
+    for G in (S.erdos_renyi(20000, 100000, seed=81, n_elabels=300), S.rmat(11, 8000, seed=82, n_elabels=3)):
+        text = G.to_g_text()
+        assert len(text) > 4 * 4096
+        d = fm.Graph.from_text(ctx, text)
+        p = tmp_path / "ok.g"
+        p.write_bytes(text)
+        fm.write_graph_cache(str(p), str(tmp_path / "ok.fmgb"))
+        h = fm.Graph.from_file(ctx, str(tmp_path / "ok.fmgb"))
+        di, hi = d.info(), h.info()
+        for f in ("vertices", "label_slots", "edges", "segments", "long_segments", "max_list", "nbr_words"):
+            assert getattr(di, f) == getattr(hi, f), f
+        for qq in (S.query_cycle(3, [1, 2, 3]), S.query_path(4, [1, 2, 1]), S.query_star(4, [2, 2, 3])):
+            q = fm.Query.from_text(qq.to_g_text())
+            assert fm.match(ctx, d, q, mode=fm.MODE_COUNT).count == fm.match(ctx, h, q, mode=fm.MODE_COUNT).count
+        d.close()
+        h.close()
