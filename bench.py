@@ -786,6 +786,55 @@ def run_skew(args, rank, world, local):
     return 0
 
 
+def run_ingest(args, rank, world, local):
+    """Ingest of the batched workload's graph as .g text (over 2 GiB): the
+    text parsed on the device (fm_graph_load_file), parsed on the host into
+    a binary cache (fm_graph_write_cache), and the cache loaded; every graph
+    must equal the one built from the edge arrays."""
+    import tempfile
+    import torch
+    import forkmatch_gb300 as fm
+    from forkmatch_gb300 import workloads as W
+    torch.cuda.set_device(local)
+    G = W.batched_graph()
+    src, dst, lab = G.directed()
+    t = time.time()
+    text = G.to_g_text()
+    text_s = time.time() - t
+    ctx = fm.Context(prealloc_bytes=2 * GB, soln_prealloc_bytes=512 << 20, output_prealloc_bytes=512 << 20,
+                     device=local)
+    ref = fm.Graph.from_edges(ctx, G.V, G.n_elabels + 1, src, dst, lab).info()
+    fields = ("vertices", "label_slots", "edges", "segments", "long_segments", "max_list", "nbr_words")
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        tp, cp = os.path.join(td, "batched.g"), os.path.join(td, "batched.fmgb")
+        with open(tp, "wb") as f:
+            f.write(text)
+        del text
+        for name, fn in (("device_parse", lambda: fm.Graph.from_file(ctx, tp)),
+                         ("host_parse_to_cache", lambda: fm.write_graph_cache(tp, cp)),
+                         ("cache_load", lambda: fm.Graph.from_file(ctx, cp))):
+            t = time.time()
+            g = fn()
+            el = time.time() - t
+            row = {"seconds": el}
+            if g is not None:
+                inf = g.info()
+                row["same_graph"] = all(getattr(inf, f) == getattr(ref, f) for f in fields)
+                row["device_build_ms"] = inf.build_ms
+                g.close()
+            out[name] = row
+        size = os.path.getsize(tp)
+    line = {"metric": "ingest GB/s (text bytes / seconds)", "value": size / out["device_parse"]["seconds"] / 1e9,
+            "unit": "GB/s", "n_gpus": 1, "higher_is_better": True, "data": "synthetic (seeded generators)",
+            "config": {"workload": "ingest", "graph": "the batched workload's R-MAT 2^22 / 64M edges as .g text",
+                       "text_bytes": size, "over_2GiB": size > (2 << 30), "text_generate_s": text_s},
+            "paths": out}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def verify_rows(ctx, g, queries, qinfo, edges, roots, sample=2048):
     """Size-independent check: sampled table rows are injective and every query
     e-line maps onto a data e-line with the same label."""
@@ -862,6 +911,8 @@ def main():
         return run_serving(args, rank, world, local)
     if args.workload == "skew":
         return run_skew(args, rank, world, local)
+    if args.workload == "ingest":
+        return run_ingest(args, rank, world, local)
     return run_ours(args, rank, world, local)
 
 
