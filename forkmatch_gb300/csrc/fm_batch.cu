@@ -81,7 +81,7 @@ using dev::seg_has;
 using dev::slot_locate;
 
 constexpr int kBWarps = 8;
-constexpr uint32_t kBStage = 256;
+constexpr uint32_t kBStage = 128;
 constexpr uint32_t kHeavyMaxPieces = 65536;
 
 struct BTune {
@@ -295,7 +295,7 @@ __device__ __forceinline__ void bdefer(const BatchParams& P, uint32_t chunk) {
 }
 
 template <bool ROOTS>
-__global__ void __launch_bounds__(kBWarps * 32, 5) k_bexpand(const __grid_constant__ BatchParams P) {
+__global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand(const __grid_constant__ BatchParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t d = P.depth;
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(kBWarps * 32, 5) k_bexpand(const __grid_consta
 }
 
 template <bool ROOTS>
-__global__ void __launch_bounds__(kBWarps * 32, 5) k_bexpand_heavy(const __grid_constant__ BatchParams P) {
+__global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand_heavy(const __grid_constant__ BatchParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned long long h = P.ctl->heavy;
     const uint32_t nent = (uint32_t)(h >> 32);
