@@ -257,12 +257,12 @@ __device__ __forceinline__ void bprocess(const BatchParams& P, const BMem& m, ui
             const uint4 ds = m.segs_s[dj * 32 + j];
             x = seg_at(ds, t, P.nbr);
             ok = true;
-            for (uint32_t c = 0; c < d && ok; c++) ok = m.rows_s[c * 32 + j] != x;
             const uint32_t k = m.k_s[j];
             for (uint32_t i = 0; i < k && ok; i++) {
                 if (i == dj) continue;
                 ok = seg_has(m.segs_s[i * 32 + j], x, 1, P.nbr, P.bm, P.bm_words);
             }
+            for (uint32_t c = 0; c < d && ok; c++) ok = m.rows_s[c * 32 + j] != x;
         }
         const bool fin = ok && m.fin_s[j];
         bfinal(P, m, fin, j, x, lane, d);

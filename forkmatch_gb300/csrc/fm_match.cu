@@ -113,20 +113,20 @@ __device__ __forceinline__ void defer_chunk(const ExpandParams& P, uint32_t chun
 }
 
 // Does driver value x (position t of parent j's driver list dj) survive?
-// Injectivity first (shared memory only), then membership in the other lists.
+// Membership in the other lists first (most candidates fail there), then
+// injectivity against the parent's row in shared memory (rarely fails).
 template <bool DUPS>
 __device__ __forceinline__ bool slot_check(const ExpandParams& P, uint32_t x, uint32_t t, uint32_t j, uint32_t dj,
                                            const uint4& ds, const uint4* segs_s, const uint32_t* rows_s,
                                            uint32_t k, uint32_t d) {
     bool ok = true;
-    for (uint32_t c = 0; c < d && ok; c++) ok = rows_s[c * 32 + j] != x;
-    if (!ok) return false;
     uint32_t need = 1;
     if (DUPS) need = seg_rank(ds, t, x, P.nbr) + 1;
     for (uint32_t i = 0; i < k && ok; i++) {
         if (i == dj) continue;
         ok = seg_has(segs_s[i * 32 + j], x, need, P.nbr, P.bm, P.bm_words);
     }
+    for (uint32_t c = 0; c < d && ok; c++) ok = rows_s[c * 32 + j] != x;
     return ok;
 }
 
