@@ -4,8 +4,9 @@ Every subtree of the search is independent and the depth-0 roots partition it
 (the reference already splits the vertex range across blocks,
 src/smsm.cu:803-811).  Each rank holds a replica of the data graph and matches
 the roots of its own range; the only exchange is a sum of per-query uint64
-counts and, in table mode, a concatenation of the row blocks.  No collective
-runs on the data path.
+counts and, in table mode, a concatenation of the row blocks.  A batch can
+instead be split by query (split_queries): each rank matches whole queries.
+No collective runs on the data path.
 """
 
 
@@ -14,6 +15,33 @@ def root_ranges(V, world):
     if world < 1:
         raise ValueError("world must be >= 1")
     return [(V * r // world, V * (r + 1) // world) for r in range(world)]
+
+
+def split_queries(costs, world):
+    """Assign the queries of a batch to ranks: greedy longest-processing-time
+    on an estimated cost per query (e.g. its recorded count or plain time).
+    Returns, per rank, the ascending list of query indices it matches.  Every
+    query goes to exactly one rank; each rank then runs its queries as one
+    batch over its graph replica, and only the per-query counts (and tables)
+    are exchanged."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    load = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in sorted(range(len(costs)), key=lambda i: (-float(costs[i]), i)):
+        r = min(range(world), key=lambda r: (load[r], r))
+        parts[r].append(i)
+        load[r] += float(costs[i])
+    return [sorted(p) for p in parts]
+
+
+def merge_query_counts(dist, n, mine, counts):
+    """Per-query counts of a query-sharded batch: rank r matched the queries
+    `mine` with results `counts`; returns all n counts on every rank."""
+    full = [0] * n
+    for i, c in zip(mine, counts):
+        full[i] = int(c)
+    return reduce_counts(dist, full)
 
 
 def reduce_counts(dist, counts):

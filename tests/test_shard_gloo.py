@@ -18,6 +18,17 @@ def test_root_ranges_partition():
             assert all(b <= e for b, e in rs)
 
 
+def test_split_queries_balances_and_covers():
+    costs = [100, 1, 1, 50, 50, 3, 7, 7, 90, 10]
+    for world in (1, 2, 3, 4, 16):
+        parts = shard.split_queries(costs, world)
+        flat = sorted(i for p in parts for i in p)
+        assert flat == list(range(len(costs)))
+        loads = [sum(costs[i] for i in p) for p in parts]
+        if world <= len(costs):
+            assert max(loads) <= sum(costs) / world + max(costs)
+
+
 def _free_port():
     s = socket.socket()
     s.bind(("127.0.0.1", 0))
@@ -65,6 +76,46 @@ def test_two_gloo_ranks_reproduce_full_result():
     q = ctx.Queue()
     port = _free_port()
     procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=180)
+    assert all(p.exitcode == 0 for p in procs), [p.exitcode for p in procs]
+    ok, total, full = q.get(timeout=10)
+    assert ok, (total, full)
+
+
+def _batch_rank_main(rank, world, port, result_q):
+    import torch.distributed as dist
+
+    from forkmatch_gb300 import synth as S
+    from oracle import oracle as O
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    G = S.erdos_renyi(300, 1500, seed=8, n_elabels=2)
+    src, dst, lab = G.directed()
+    og = O.Graph.from_edges(G.V, 3, src, dst, lab)
+    queries = [S.query_cycle(4, [1, 2, 1, 2]), S.query_path(4, [1, 1, 2]), S.query_cycle(3, [1, 1, 2]),
+               S.query_star(4, [1, 2, 2]), S.query_path(3, [2, 2]), S.query_clique(4, [1, 2])]
+    plans = [O.plan(qq.to_g_text(), enumerate_aut=0) for qq in queries]
+    costs = [len(qq.edges) for qq in queries]
+    mine = shard.split_queries(costs, world)[rank]
+    counts = [O.match(og, plans[i], threads=1)[0] for i in mine]
+    total = shard.merge_query_counts(dist, len(queries), mine, counts)
+    if rank == 0:
+        full = [O.match(og, p, threads=1)[0] for p in plans]
+        result_q.put((total == full, total, full))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_split_a_batch_by_query():
+    mp = pytest.importorskip("torch.multiprocessing")
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_batch_rank_main, args=(r, 2, port, q)) for r in range(2)]
     for p in procs:
         p.start()
     for p in procs:
