@@ -58,6 +58,7 @@ def parse_args():
     ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--max-batch", type=int, default=32)
     ap.add_argument("--pool-gb", type=int, default=120)
+    ap.add_argument("--serving-max-ms", type=float, default=20.0, help="latency bound of the query screen")
     ap.add_argument("--skew-limit", type=int, default=1 << 36, help="work limit per query of the skew workload")
     return ap.parse_args()
 
@@ -655,7 +656,7 @@ def run_serving(args, rank, world, local):
         text = qq.to_g_text()
         q = fm.Query.from_text(text)
         r = fm.match(ctx, g, q, mode=fm.MODE_COUNT, work_limit=1 << 25, allow_limit=True)
-        if r.status != fm.FM_OK or r.device_ms > 20.0:
+        if r.status != fm.FM_OK or r.device_ms > args.serving_max_ms:
             continue
         queries.append(q)
         texts.append(text)
@@ -708,7 +709,7 @@ def run_serving(args, rank, world, local):
                        "edges, 64 edge labels, 8 vertex labels uniform" % (scale, m // 1000000),
                        "queries": len(queries), "query_vertices": "%d-%d" % (min(sizes), max(sizes)),
                        "screening": "walk-induced subgraphs; kept when the plain count finishes within a work "
-                                    "limit of 2^25 embeddings / partial matches and 20 ms",
+                                    "limit of 2^25 embeddings / partial matches and %g ms" % args.serving_max_ms,
                        "pool_gb": args.pool_gb, "slots": args.slots, "max_batch": args.max_batch,
                        "arrivals": "Poisson, %g s or %d requests per rate" % (args.serving_seconds,
                                                                              args.serving_requests)},
