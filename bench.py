@@ -663,6 +663,8 @@ def run_serving(args, rank, world, local):
         alone.append(r.count)
         alone_ms.append(r.device_ms)
     screen_s = time.time() - t
+    if not queries:
+        raise SystemExit("no candidate query passed the screen (work limit 2^25, %g ms)" % args.serving_max_ms)
     sizes = [qu.q for qu in queries]
 
     srv = fm.Server(ctx, g, slots=args.slots, max_batch=args.max_batch)
