@@ -197,7 +197,9 @@ def run_reference(args, rank, world):
     og = O.Graph.from_edges(G.V, G.n_elabels + 1, src, dst, lab)
     plans = [O.plan(q["text"].encode(), enumerate_aut=0) for q in wl["queries"]]
     threads = os.cpu_count() or 1
-    frac = 256 if args.workload == "batched" else 16
+    # a contiguous root range; per-root work is heavy-tailed (hubs), so the
+    # sample is a quarter of the vertices (about 2 s on 16 cores per step)
+    frac = 256 if args.workload == "batched" else 4
     sample_roots = G.V // frac
 
     def step():
