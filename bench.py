@@ -237,7 +237,7 @@ def workload_config(wl, G, same):
                          "spanning trees have ~1e16 embeddings and are not enumerable)",
             "mode": "plain: one query per launch sequence, full uint32 embedding tables",
             "graph_matches_recorded_hash": same,
-            "l2": "inputs larger than L2: resident graph ~0.6 GB vs 129 MB L2; no flush between steps"}
+            "l2": "inputs larger than L2: resident graph 1.6 GB (records, lists, bitmaps) vs 129 MB L2, 10.6 GB of table rows written per step; no flush between steps"}
 
 
 # ------------------------------------------------------------------ our arm
@@ -457,7 +457,7 @@ def batched_config(wl, G, same):
                     "split granularity and grid; per-query uint64 counts + uint32 tables. plain: one fm_match "
                     "per query (table mode)",
             "graph_matches_recorded_hash": same,
-            "l2": "inputs larger than L2: resident graph ~2.6 GB vs 129 MB L2; no flush between steps"}
+            "l2": "inputs larger than L2: resident graph 5.7 GB vs 129 MB L2; no flush between steps"}
 
 
 def run_batched(args, rank, world, local):
