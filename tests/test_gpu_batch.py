@@ -153,3 +153,34 @@ def test_batch_fallback_duplicates_and_single_vertex(env):
     assert st.single_queries == 3
     assert counts == [fm.match(ctx, g, q, mode=fm.MODE_COUNT).count for q in qs]
     b.close()
+
+
+def test_batch_with_list_bitmaps(monkeypatch):
+    """The batch kernels answer membership from list bitmaps too (lists down
+    to 4 entries get one here); counts equal the oracle's."""
+    monkeypatch.setenv("FM_BITMAP_MIN_LEN", "4")
+    ctx = fm.Context(prealloc_bytes=3 << 30, soln_prealloc_bytes=1 << 30, output_prealloc_bytes=1 << 30,
+                     bank_rows=1024)
+    G = S.rmat(12, 30000, seed=91, n_elabels=3)
+    src, dst, lab = G.directed()
+    g = fm.Graph.from_edges(ctx, G.V, 4, src, dst, lab)
+    assert g.info().bitmaps > 0
+    og = O.Graph.from_edges(G.V, 4, src, dst, lab)
+    rng = np.random.default_rng(92)
+    qs, want = [], []
+    while len(qs) < 16:
+        k = int(rng.integers(3, 7))
+        q = S.query_random_walk(G, k, rng, bias=1.0)
+        if q is None:
+            continue
+        try:
+            c = O.match(og, O.plan(q.to_g_text(), enumerate_aut=0), limit=1 << 22, scan_limit=1 << 26)[0]
+        except O.OracleError:
+            continue
+        qs.append(fm.Query.from_text(q.to_g_text()))
+        want.append(c)
+    b = fm.Batch(ctx, g, qs, mode=fm.MODE_COUNT)
+    assert b.run()[0] == want
+    b.close()
+    g.close()
+    ctx.close()
