@@ -202,15 +202,20 @@ __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem
     return __shfl_sync(kFull, incl, 31);
 }
 
+// Staged survivors go to the next level; a parent's columns come from the
+// warp's shared-memory copy of chunk `cur` when the parent belongs to it.
 template <bool ROOTS>
-__device__ __forceinline__ void bflush(const BatchParams& P, const BMem& m, uint32_t nst, uint32_t lane, uint32_t d) {
+__device__ __forceinline__ void bflush(const BatchParams& P, const BMem& m, uint32_t nst, uint32_t lane, uint32_t d,
+                                       uint32_t cur) {
     unsigned long long pos0 = 0;
     if (lane == 0) pos0 = atomicAdd(&P.ctl->produced, (unsigned long long)nst);
     pos0 = __shfl_sync(kFull, pos0, 0);
     for (uint32_t c = 0; c < d; c++) {
         uint32_t* col = P.pout + c * P.ocap + pos0;
-        for (uint32_t i = lane; i < nst; i += 32)
-            col[i] = ROOTS ? m.stp[i] : __ldg(P.pin + c * P.pstride + m.stp[i]);
+        for (uint32_t i = lane; i < nst; i += 32) {
+            const uint32_t p = m.stp[i];
+            col[i] = ROOTS ? p : ((p >> 5) == cur ? m.rows_s[c * 32 + (p & 31)] : __ldg(P.pin + c * P.pstride + p));
+        }
     }
     uint32_t* colx = P.pout + d * P.ocap + pos0;
     uint32_t* colq = P.pout + (d + 1) * P.ocap + pos0;
@@ -244,8 +249,8 @@ __device__ __forceinline__ void bfinal(const BatchParams& P, const BMem& m, bool
 }
 
 template <bool ROOTS>
-__device__ __forceinline__ void bprocess(const BatchParams& P, const BMem& m, uint32_t begin, uint32_t end,
-                                         uint32_t lane, uint32_t d, uint32_t& nst) {
+__device__ __forceinline__ void bprocess(const BatchParams& P, const BMem& m, uint32_t chunk, uint32_t begin,
+                                         uint32_t end, uint32_t lane, uint32_t d, uint32_t& nst) {
     for (uint32_t base = begin; base < end; base += 32) {
         const uint32_t s = base + lane;
         bool ok = false;
@@ -277,7 +282,7 @@ __device__ __forceinline__ void bprocess(const BatchParams& P, const BMem& m, ui
         nst += __popc(b);
         if (nst > kBStage - 32) {
             __syncwarp();
-            bflush<ROOTS>(P, m, nst, lane, d);
+            bflush<ROOTS>(P, m, nst, lane, d, chunk);
             nst = 0;
         }
         __syncwarp();
@@ -303,6 +308,7 @@ __global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand(const __grid_consta
     const BTune T = make_btune(P);
     unsigned long long n_lookups = 0, n_words = 0, n_parents = 0, credit = 0;
     uint32_t nst = 0;
+    uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
     for (;;) {
         unsigned long long item = 0;
         if (lane == 0) item = atomicAdd(&P.ctl->claim, 1ull);
@@ -320,6 +326,7 @@ __global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand(const __grid_consta
         uint32_t k;
         unsigned long long w;
         const uint32_t total = bload_chunk<ROOTS>(P, m, chunk, lane, d, T.n_parents, valid, k, w);
+        last_chunk = chunk;
         // only survivors of queries that go on use the next level's buffer;
         // the upper bound of the whole chunk is reserved (over-reserving is safe)
         if (total && P.pout) {
@@ -363,11 +370,11 @@ __global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand(const __grid_consta
             pub = __shfl_sync(kFull, pub, 0);
             if (pub) continue;
         }
-        bprocess<ROOTS>(P, m, 0, total, lane, d, nst);
+        bprocess<ROOTS>(P, m, chunk, 0, total, lane, d, nst);
         // the stage refers to this chunk's query ids only through stq, and to
         // its parents through pidx: it can outlive the chunk
     }
-    if (nst) bflush<ROOTS>(P, m, nst, lane, d);
+    if (nst) bflush<ROOTS>(P, m, nst, lane, d, last_chunk);
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
         n_lookups += __shfl_down_sync(kFull, n_lookups, o);
@@ -393,6 +400,7 @@ __global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand_heavy(const __grid_
     const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax);
     const BTune T = make_btune(P);
     uint32_t nst = 0;
+    uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
     for (;;) {
         unsigned long long gp = 0;
         if (lane == 0) gp = atomicAdd(&P.ctl->claim2, 1ull);
@@ -411,9 +419,10 @@ __global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand_heavy(const __grid_
         uint32_t k;
         unsigned long long w;
         bload_chunk<ROOTS>(P, m, e.chunk, lane, d, T.n_parents, valid, k, w);
-        bprocess<ROOTS>(P, m, begin, end, lane, d, nst);
+        last_chunk = e.chunk;
+        bprocess<ROOTS>(P, m, e.chunk, begin, end, lane, d, nst);
     }
-    if (nst) bflush<ROOTS>(P, m, nst, lane, d);
+    if (nst) bflush<ROOTS>(P, m, nst, lane, d, last_chunk);
 }
 
 cudaError_t launch_batch_level(const BatchParams& p, bool roots, int grid, int heavy_grid, size_t smem,
