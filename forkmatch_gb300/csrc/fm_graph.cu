@@ -108,14 +108,15 @@ __global__ void k_copy_long(const uint64_t* __restrict__ keys, const uint32_t* _
 }
 
 // Source vertex of each segment (segments are in (label, src) order) and the
-// number of segments per label.
+// first segment of every label that has one (one writer per label).
 __global__ void k_seg_heads(const uint64_t* __restrict__ keys, const uint64_t* __restrict__ seg_start, uint64_t nseg,
-                            uint32_t vbits, uint32_t* __restrict__ heads, unsigned int* __restrict__ per_label) {
+                            uint32_t vbits, uint32_t* __restrict__ heads, unsigned long long* __restrict__ first) {
     const uint64_t vmask = (1ull << vbits) - 1;
     for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < nseg; s += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t k = keys[seg_start[s]];
         heads[s] = (uint32_t)((k >> vbits) & vmask);
-        atomicAdd(per_label + (uint32_t)(k >> (2 * vbits)), 1u);
+        const uint32_t l = (uint32_t)(k >> (2 * vbits));
+        if (s == 0 || (uint32_t)(keys[seg_start[s - 1]] >> (2 * vbits)) != l) first[l] = s;
     }
 }
 
@@ -302,16 +303,17 @@ fm_status build_device_graph(DeviceGraph& g, uint32_t V, uint32_t L, uint64_t E,
         FM_CUDA(cudaGetLastError());
         DevBuf per_label;
         FM_CUDA(cudaMalloc(&g.heads, nseg * 4));
-        FM_CUDA(cudaMalloc(&per_label.p, (size_t)L * 4));
-        FM_CUDA(cudaMemsetAsync(per_label.p, 0, (size_t)L * 4, s));
+        FM_CUDA(cudaMalloc(&per_label.p, (size_t)L * 8));
+        FM_CUDA(cudaMemsetAsync(per_label.p, 0xff, (size_t)L * 8, s));
         k_seg_heads<<<grid_for(nseg, sms), 256, 0, s>>>(sorted, seg_start.as<uint64_t>(), nseg, vbits, g.heads,
-                                                       per_label.as<unsigned int>());
+                                                       per_label.as<unsigned long long>());
         FM_CUDA(cudaGetLastError());
-        std::vector<uint32_t> cnt(L);
-        FM_CUDA(cudaMemcpyAsync(cnt.data(), per_label.p, (size_t)L * 4, cudaMemcpyDeviceToHost, s));
+        std::vector<unsigned long long> first(L);
+        FM_CUDA(cudaMemcpyAsync(first.data(), per_label.p, (size_t)L * 8, cudaMemcpyDeviceToHost, s));
         FM_CUDA(cudaStreamSynchronize(s));
-        g.head_off.assign(L + 1, 0);
-        for (uint32_t l = 0; l < L; l++) g.head_off[l + 1] = g.head_off[l] + cnt[l];
+        // a label without segments starts where the next label with one does
+        g.head_off.assign(L + 1, nseg);
+        for (uint32_t l = L; l-- > 0;) g.head_off[l] = first[l] != ~0ull ? first[l] : g.head_off[l + 1];
 
         // membership bitmaps for the longest lists (not with duplicates: a
         // bit cannot count copies; vertex ids must leave bit 31 of z free)
