@@ -2,6 +2,12 @@
 plain-at-scale workload, with full uint32 embedding tables.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --workload batched|serving|skew|ingest     (one GPU each)
+
+The other workloads: batched (512 queries, batched vs plain form), serving
+(Poisson arrivals against a resident 2^24-vertex graph, p50/p99), skew
+(count-only stress on a Chung-Lu graph with work limits), ingest (the batched
+graph as >2 GiB .g text); see forkmatch_gb300/workloads.py.
 
 Workload (forkmatch_gb300.workloads): R-MAT 2^20 vertices, 16M undirected
 edges (32M e-lines), 32 edge labels; 16 queries of 8 vertices recorded in
