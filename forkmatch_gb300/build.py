@@ -20,7 +20,7 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "
                   "--expt-relaxed-constexpr"]
 SOURCES = ["fm_host.cu", "fm_match.cu", "fm_graph.cu", "fm_parse.cpp", "fm_static.cu", "fm_batch.cu",
            "fm_serve.cpp", "fm_table.cpp", "fm_ingest.cu"]
-HEADERS = ["fm_internal.h", "fm_device.cuh"]
+HEADERS = ["fm_internal.h", "fm_device.cuh", "fm_pool.h"]
 
 
 def _nvcc():

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "fm_internal.h"
+#include "fm_pool.h"
 
 using namespace fm;
 
@@ -46,60 +47,6 @@ uint64_t round_up(uint64_t x, uint64_t g) { return (x + g - 1) / g * g; }
 double ms_between(Clock::time_point a, Clock::time_point b) {
     return std::chrono::duration<double, std::milli>(b - a).count();
 }
-
-// First fit over [0, size) with coalescing frees.
-class PoolAlloc {
-public:
-    void init(uint64_t size) {
-        free_.clear();
-        if (size) free_[0] = size;
-        total_ = free_bytes_ = size;
-        peak_ = 0;
-    }
-    bool alloc(uint64_t bytes, uint64_t& off) {
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second < bytes) continue;
-            off = it->first;
-            const uint64_t rest = it->second - bytes;
-            free_.erase(it);
-            if (rest) free_[off + bytes] = rest;
-            free_bytes_ -= bytes;
-            peak_ = std::max(peak_, total_ - free_bytes_);
-            return true;
-        }
-        return false;
-    }
-    void release(uint64_t off, uint64_t bytes) {
-        free_bytes_ += bytes;
-        auto next = free_.lower_bound(off);
-        if (next != free_.begin()) {
-            auto prev = std::prev(next);
-            if (prev->first + prev->second == off) {
-                off = prev->first;
-                bytes += prev->second;
-                free_.erase(prev);
-            }
-        }
-        next = free_.lower_bound(off);
-        if (next != free_.end() && off + bytes == next->first) {
-            bytes += next->second;
-            free_.erase(next);
-        }
-        free_[off] = bytes;
-    }
-    uint64_t largest() const {
-        uint64_t m = 0;
-        for (const auto& f : free_) m = std::max(m, f.second);
-        return m;
-    }
-    uint64_t free_bytes() const { return free_bytes_; }
-    uint64_t total() const { return total_; }
-    uint64_t peak() const { return peak_; }
-
-private:
-    std::map<uint64_t, uint64_t> free_;
-    uint64_t total_ = 0, free_bytes_ = 0, peak_ = 0;
-};
 
 struct Request {
     uint64_t ticket = 0;
@@ -133,7 +80,7 @@ struct fm_server {
     const fm_graph* graph = nullptr;
     fm_server_opts opts{};
     char* base = nullptr;           // lease pool
-    PoolAlloc pool;
+    fm::PoolAlloc pool;
     uint64_t min_rows = 0;          // one 32-parent chunk of the longest list, plus one bank
     struct Slot {
         fm_context* ctx = nullptr;
