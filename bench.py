@@ -66,6 +66,7 @@ def parse_args():
     ap.add_argument("--pool-gb", type=int, default=120)
     ap.add_argument("--serving-max-ms", type=float, default=20.0, help="latency bound of the query screen")
     ap.add_argument("--skew-limit", type=int, default=1 << 36, help="work limit per query of the skew workload")
+    ap.add_argument("--soln-gb", type=float, default=24.0, help="SOLN_PREALLOC of the plain-at-scale context, GiB")
     return ap.parse_args()
 
 
@@ -260,7 +261,7 @@ def run_ours(args, rank, world, local):
     max_count = max(q["count"] for q in queries_meta)
     out_bytes = ((int(max_count * 8 * 4 * 1.05) + (64 << 20)) >> 20) << 20
     # the slab beyond SOLN + OUTPUT is the pool of the served e2e path
-    ctx = fm.Context(prealloc_bytes=64 * GB, soln_prealloc_bytes=24 * GB,
+    ctx = fm.Context(prealloc_bytes=64 * GB, soln_prealloc_bytes=int(args.soln_gb * GB),
                      output_prealloc_bytes=out_bytes, bank_rows=1 << 16, device=local)
     t = time.time()
     g = fm.Graph.from_edges(ctx, G.V, G.n_elabels + 1, src, dst, lab)
