@@ -468,3 +468,41 @@ def test_device_parser_agrees_with_host_parser(ctx, tmp_path):
             assert fm.match(ctx, d, q, mode=fm.MODE_COUNT).count == fm.match(ctx, h, q, mode=fm.MODE_COUNT).count
         d.close()
         h.close()
+
+
+@pytest.mark.parametrize("data,query,code", [
+    (None, b"ok", 12),
+    (b"t # 1\n2 0 1 1\nt # -1", b"ok", 76),
+    (b"t # 0\n2 0 1 1\nt # -2", b"ok", 77),
+    (b"t # 0\n2 x 1 1\nt # -1", b"ok", 78),
+    (b"t # 0\n2 2 1 1\nv 0 1\nv 1 1\ne 0 1 1\nx 1 0 1\nt # -1", b"ok", 79),
+    (b"ok", None, 232),
+    (b"ok", b"t # 0\n2 2 1 1\nv 0 1\nv x 1\ne 0 1 1\ne 1 0 1\nt # -1", 233),
+    (b"ok", b"t # 0\n3 2 1 1\nv 0 1\nv 1 1\ne 0 1 1\ne 1 0 1\nt # -1", 234),
+    (b"ok", b"t # 0\n4 4 1 1\nv 0 1\nv 1 1\nv 2 1\nv 3 1\ne 0 1 1\ne 1 0 1\ne 2 3 1\ne 3 2 1\nt # -1", 1),
+])
+def test_cli_exit_codes(tmp_path, data, query, code):
+    """The CLI maps every input error to the reference's exit code; the
+    oracle's parsers give the same codes for the same texts."""
+    import subprocess
+    good_data = S.erdos_renyi(50, 120, seed=3, n_elabels=2).to_g_text()
+    good_query = S.query_path(3, [1, 2]).to_g_text()
+    d = tmp_path / "d.g"
+    q = tmp_path / "q.g"
+    if data is not None:
+        d.write_bytes(good_data if data == b"ok" else data)
+    if query is not None:
+        q.write_bytes(good_query if query == b"ok" else query)
+    env = dict(os.environ, FM_PREALLOC=str(1 << 30), FM_SOLN_PREALLOC=str(256 << 20),
+               FM_OUTPUT_PREALLOC=str(256 << 20))
+    r = subprocess.run([os.path.join(os.path.dirname(fm.LIB_PATH), "ForkMatch"), str(q), str(d)],
+                       capture_output=True, text=True, env=env)
+    assert r.returncode == code, r.stdout + r.stderr
+    if data not in (None, b"ok"):
+        with pytest.raises(O.OracleError) as ei:
+            O.Graph.parse(data)
+        assert ei.value.code == code
+    if query not in (None, b"ok") and code != 1:
+        with pytest.raises(O.OracleError) as ei:
+            O.plan(query)
+        assert ei.value.code == code
