@@ -222,10 +222,12 @@ fm_status fm_match(fm_context* ctx, const fm_graph* g, const fm_query* q,
  * per program run (src/smsm.cu:1182-1349): a batch matches many compiled
  * queries against one resident graph in shared level launches (max(q) - 1 of
  * them, captured once as a CUDA graph and replayed), each query's results
- * identical to fm_match's.  Table mode gives every query an equal share of
- * OUTPUT_PREALLOC (FM_ERR_OUTPUT_OVERFLOW if one overflows; counts stay
- * exact).  Queries with one vertex, and every query on a graph with duplicate
- * e-lines, are matched one by one through fm_match (count only). */
+ * identical to fm_match's.  In table mode the first run counts every query
+ * (a counting replay) and then gives each one a table region of exactly its
+ * size in OUTPUT_PREALLOC, in batch order while it lasts (a query that does
+ * not fit gets FM_ERR_OUTPUT_OVERFLOW; counts stay exact).  Queries with one
+ * vertex, and every query on a graph with duplicate e-lines, are matched one
+ * by one through fm_match (count only). */
 typedef struct fm_batch fm_batch;
 typedef struct fm_batch_stats {
     uint64_t embeddings;        /* sum of the counts */
