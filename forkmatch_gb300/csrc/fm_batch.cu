@@ -743,7 +743,8 @@ fm_status batch_create_impl(fm_context* ctx, const fm_graph* graph, const fm_que
         plans.push_back(bp);
         table_words += pl.q;
     }
-    // table regions: the same number of rows for every batched query
+    // provisional table regions (the same number of rows for every batched
+    // query); the first table run replaces them with exact ones
     const uint64_t rows_each = table_words ? cv.output_bytes / 4 / table_words : 0;
     uint64_t off = 0;
     for (auto& bp : plans) {
