@@ -53,6 +53,24 @@ fm_status scratch_for_device(int dev, unsigned char** out) {
     return FM_OK;
 }
 
+// Makes a device current for the scope of one call and restores the
+// caller's current device when the scope ends.
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t enter(int dev) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) {
+            prev = -1;
+            return e;
+        }
+        return prev == dev ? cudaSuccess : cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
 struct StaticRun {
     cudaStream_t s;
     int sms;
@@ -75,8 +93,12 @@ struct StaticRun {
         uint64_t fresh = 0;
         const size_t smem = expand_smem_bytes(d, nreq[d], block / 32);
         const int per_sm = expand_blocks_per_sm(mode, roots, dups, smem, block);
-        // a bounded grid keeps the deferred lists small: at most warps * 8 entries
-        const int full = std::min(sms * per_sm, sms * 2);
+        // A launch defers at most 8 chunks per warp (the largest claim batch),
+        // so a grid of at most kStaticDefCap / (8 * warps per block) blocks
+        // keeps one launch's deferred chunks within a list whatever the SM
+        // count; the carried-over entries are checked on the host below.
+        const int def_bound = (int)(kStaticDefCap / (8u * (uint32_t)(block / 32)));
+        const int full = std::max(1, std::min(std::min(sms * per_sm, sms * 2), def_bound));
         while (true) {
             const uint64_t items = ndef_in + (n_chunks - fresh);
             if (items == 0) break;
@@ -149,7 +171,9 @@ extern "C" fm_status fm_match_static(const fm_graph* graph, const fm_query* quer
     if (rows_written) *rows_written = 0;
     const DeviceGraph& g = graph->g;
     const Plan& pl = query->p;
-    FM_CUDA(cudaSetDevice(g.device));
+    // the caller's current device is restored on every return path
+    DeviceGuard guard;
+    FM_CUDA(guard.enter(g.device));
     unsigned char* scratch = nullptr;
     fm_status st = scratch_for_device(g.device, &scratch);
     if (st != FM_OK) return st;

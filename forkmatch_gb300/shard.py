@@ -17,6 +17,39 @@ def root_ranges(V, world):
     return [(V * r // world, V * (r + 1) // world) for r in range(world)]
 
 
+def root_work_weights(src, V):
+    """Estimated search work of each root vertex: d(v)^2 + 1, where d(v) is its
+    number of e-lines (the partial matches two levels below a root grow with
+    the square of its degree; the 1 charges the root lookup itself)."""
+    import numpy as np
+    d = np.bincount(np.asarray(src, dtype=np.int64), minlength=V).astype(np.float64)
+    return d * d + 1.0
+
+
+def root_ranges_weighted(weights, world):
+    """Contiguous root ranges [b, e), one per rank, covering [0, len(weights)),
+    cut where the prefix sum of the per-root work estimate crosses r/world of
+    the total.  On R-MAT-like graphs, where a few hubs hold most of the work,
+    equal-length ranges leave one rank with the hubs; these ranges give every
+    rank about the same estimated work (each within one root's weight of
+    total/world)."""
+    import numpy as np
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    w = np.asarray(weights, dtype=np.float64)
+    V = len(w)
+    if V == 0:
+        return [(0, 0)] * world
+    c = np.cumsum(w)
+    total = c[-1]
+    cuts = [0]
+    for r in range(1, world):
+        # first root whose inclusive prefix reaches r/world of the work
+        cuts.append(int(min(V, max(cuts[-1], np.searchsorted(c, total * r / world, side="left") + 1))))
+    cuts.append(V)
+    return [(cuts[r], cuts[r + 1]) for r in range(world)]
+
+
 def split_queries(costs, world):
     """Assign the queries of a batch to ranks: greedy longest-processing-time
     on an estimated cost per query (e.g. its recorded count or plain time).

@@ -6,6 +6,10 @@
   compiled from the ForkMatch sources where they lie (``<ref>/src``) together
   with ``ref_planner_probe.cu``.  It is built only when the reference tree is
   present; nothing at run time depends on it.
+* ``oracle/_ref/ref_matcher`` is the reference's own GPU matcher built without
+  SYMMETRY behind ``ref_matcher_probe.cu``; it generates the golden fixture
+  ``tests/golden/ref_matches.json`` on a GPU (``tests/golden/make_ref_matches.py``)
+  and is never run by tests or the benchmark.
 
 Outputs are git-ignored.  Run ``python oracle/build.py`` or call ``build()``.
 """
@@ -15,7 +19,11 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("FM_REFERENCE_SRC", "/root/reference/src")
+# The ForkMatch checkout these recipes read: $FM_REFERENCE_ROOT, else the
+# build container's read-only mount.  It is absent on the GPU machine, where only
+# the outputs already staged under oracle/_ref/ are used.
+REF_ROOT = os.environ.get("FM_REFERENCE_ROOT", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src")
 
 
 def _run(cmd):
@@ -51,9 +59,49 @@ def build_ref_planner():
     return out
 
 
+# The reference sources the matcher probe needs, staged into oracle/_ref/src
+# (git-ignored, like every output of these recipes) so that the probe can be
+# compiled on a machine without the reference checkout (the GPU machine has
+# another CPU architecture, so nothing compiled here runs there).
+REF_FILES = ("smsm.cu", "smsm.cuh", "trie.cuh", "ccsr.cuh", "hostparser.cuh", "intersect.cuh", "tbs.cuh",
+             "environment.cuh")
+
+
+def stage_reference_sources():
+    """Copy the reference's src/ files the matcher probe includes into
+    oracle/_ref/src; returns that folder, or None without a reference checkout."""
+    if not os.path.isdir(REF_SRC):
+        return None
+    dst = os.path.join(HERE, "_ref", "src")
+    os.makedirs(dst, exist_ok=True)
+    for name in REF_FILES:
+        shutil.copyfile(os.path.join(REF_SRC, name), os.path.join(dst, name))
+    return dst
+
+
+def build_ref_matcher():
+    """Compile the reference's own GPU matcher (SYMMETRY undefined) behind
+    ref_matcher_probe.cu into oracle/_ref/ref_matcher, from the reference
+    checkout or from the staged copy; returns its path or None."""
+    src = REF_SRC if os.path.isdir(REF_SRC) else os.path.join(HERE, "_ref", "src")
+    if not os.path.isfile(os.path.join(src, "smsm.cu")) or shutil.which("nvcc") is None:
+        return None
+    out = os.path.join(HERE, "_ref", "ref_matcher")
+    probe = os.path.join(HERE, "ref_matcher_probe.cu")
+    if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(probe):
+        return out
+    # the reference's own build line (build.sh) retargeted to sm_103a, without
+    # --keep (compiler intermediates are not kept)
+    _run(["nvcc", "-rdc=true", "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler",
+          "-std=c++20 -O3 -fpermissive -w", "-std", "c++20", "-cudart", "static", "-maxrregcount=64", "-w",
+          "-I" + src, probe, "-o", out])
+    return out
+
+
 def build():
     build_oracle()
     build_ref_planner()
+    stage_reference_sources()
 
 
 if __name__ == "__main__":

@@ -35,7 +35,7 @@ from forkmatch_gb300 import synth as S  # noqa: E402
 from oracle import build as OB  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-REF_QUERIES = os.environ.get("FM_REFERENCE_QUERIES", "/root/reference/dataset/query")
+REF_QUERIES = os.path.join(OB.REF_ROOT, "dataset", "query")
 
 
 def run_ref_planner(exe, text, timeout=60):

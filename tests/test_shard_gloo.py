@@ -1,6 +1,7 @@
 """The multi-rank path on CPU: two gloo ranks, each matching its root range
-(with the oracle standing in for the GPU matcher), must reproduce the full
-count and the full table exactly."""
+(with the oracle standing in for the GPU matcher, which needs a GPU), must
+reproduce the full count and the full table exactly; the work-weighted root
+split covers every root once and balances the estimated work on R-MAT."""
 import os
 import socket
 
@@ -16,6 +17,30 @@ def test_root_ranges_partition():
             assert len(rs) == world and rs[0][0] == 0 and rs[-1][1] == V
             assert all(rs[i][1] == rs[i + 1][0] for i in range(world - 1))
             assert all(b <= e for b, e in rs)
+
+
+def test_weighted_root_ranges_cover_and_balance_on_rmat():
+    import numpy as np
+
+    from forkmatch_gb300 import synth as S
+    G = S.rmat(14, 120000, 11, 4)
+    src, _, _ = G.directed()
+    w = shard.root_work_weights(src, G.V)
+    for world in (1, 2, 3, 4, 8, 16):
+        rs = shard.root_ranges_weighted(w, world)
+        assert len(rs) == world and rs[0][0] == 0 and rs[-1][1] == G.V
+        assert all(rs[i][1] == rs[i + 1][0] for i in range(world - 1))
+        assert all(b <= e for b, e in rs)
+        covered = np.zeros(G.V, dtype=np.int64)
+        for b, e in rs:
+            covered[b:e] += 1
+        assert (covered == 1).all()
+        loads = np.array([w[b:e].sum() for b, e in rs])
+        assert loads.max() <= w.sum() / world + w.max() + 1e-6
+    # equal-length ranges put the hubs' work on few ranks; the weighted split does not
+    eq = [w[b:e].sum() for b, e in shard.root_ranges(G.V, 8)]
+    wt = [w[b:e].sum() for b, e in shard.root_ranges_weighted(w, 8)]
+    assert max(wt) <= max(eq)
 
 
 def test_split_queries_balances_and_covers():
@@ -49,7 +74,7 @@ def _rank_main(rank, world, port, result_q):
     src, dst, lab = G.directed()
     og = O.Graph.from_edges(G.V, 3, src, dst, lab)
     queries = [S.query_cycle(4, [1, 2, 1, 2]), S.query_path(4, [1, 1, 2]), S.query_cycle(3, [1, 1, 2])]
-    b, e = shard.root_ranges(G.V, world)[rank]
+    b, e = shard.root_ranges_weighted(shard.root_work_weights(src, G.V), world)[rank]
     counts, tables = [], []
     for qq in queries:
         p = O.plan(qq.to_g_text(), enumerate_aut=0)
