@@ -16,11 +16,14 @@ CLI_PATH = os.path.join(HERE, "lib", "ForkMatch")
 MAXQ = 32
 
 FM_OK = 0
+FM_ERR_POOL = 11
 FM_ERR_OUTPUT_OVERFLOW = 12
+FM_ERR_DEVICE = 14
 FM_ERR_LIMIT = 16
 MODE_TABLE, MODE_COUNT = 0, 1
 COLUMNS_REFERENCE, COLUMNS_QUERY_ID = 0, 1
 ORDER_AUTO, ORDER_REFERENCE = 0, 1
+ENGINE_PERSISTENT, ENGINE_LEVELS = 0, 1
 
 STATUS_NAMES = {
     0: "FM_OK", 1: "FM_ERR_ARG", 2: "FM_ERR_IO", 3: "FM_ERR_DATA_HEADER0", 4: "FM_ERR_DATA_TRAILER",
@@ -38,7 +41,7 @@ EXPORTS = [
     "fm_match_static", "fm_batch_create", "fm_batch_run", "fm_batch_rows", "fm_batch_copy_rows", "fm_batch_tune",
     "fm_batch_free", "fm_batch_copy_tables", "fm_server_create", "fm_server_submit", "fm_server_poll",
     "fm_server_release", "fm_server_get_stats", "fm_server_destroy", "fm_graph_write_cache", "fm_table_write",
-    "fm_table_to_query_columns",
+    "fm_table_to_query_columns", "fm_batch_set_engine",
 ]
 
 
@@ -70,7 +73,9 @@ class MatchOpts(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("columns", ctypes.c_int32), ("stream", ctypes.c_void_p),
                 ("host_rows", ctypes.c_void_p), ("host_rows_cap", ctypes.c_uint64),
                 ("root_begin", ctypes.c_uint32), ("root_end", ctypes.c_uint32), ("profile", ctypes.c_int32),
-                ("order", ctypes.c_int32), ("host_direct", ctypes.c_int32), ("work_limit", ctypes.c_uint64)]
+                ("order", ctypes.c_int32), ("host_direct", ctypes.c_int32), ("work_limit", ctypes.c_uint64),
+                ("engine", ctypes.c_int32), ("wait_limit_ms", ctypes.c_uint32),
+                ("test_stall_barrier", ctypes.c_int32)]
 
 
 class LevelStats(ctypes.Structure):
@@ -82,13 +87,15 @@ class Result(ctypes.Structure):
     _fields_ = [("count", ctypes.c_uint64), ("rows", ctypes.c_uint64), ("rows_device", ctypes.c_void_p),
                 ("rows_copied", ctypes.c_uint64), ("truncated", ctypes.c_int32), ("q", ctypes.c_uint32),
                 ("device_ms", ctypes.c_double), ("launches", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64),
-                ("d2h_bytes", ctypes.c_uint64), ("level", LevelStats * MAXQ)]
+                ("d2h_bytes", ctypes.c_uint64), ("level", LevelStats * MAXQ), ("engine", ctypes.c_int32),
+                ("passes", ctypes.c_uint32), ("max_wait_ns", ctypes.c_uint64)]
 
 
 class BatchStats(ctypes.Structure):
     _fields_ = [("embeddings", ctypes.c_uint64), ("launches", ctypes.c_uint64), ("wall_ms", ctypes.c_double),
                 ("batched_queries", ctypes.c_uint32), ("single_queries", ctypes.c_uint32),
-                ("piece_shift", ctypes.c_uint32), ("grid_quarters", ctypes.c_uint32)]
+                ("piece_shift", ctypes.c_uint32), ("grid_quarters", ctypes.c_uint32),
+                ("level_rows", ctypes.c_uint64), ("persistent", ctypes.c_int32), ("graph", ctypes.c_int32)]
 
 
 class ServerOpts(ctypes.Structure):
@@ -146,6 +153,7 @@ def lib():
         L.fm_match_static.argtypes = [vp, vp, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64), vp]
         L.fm_batch_create.argtypes = [vp, vp, ctypes.POINTER(vp), u32, i32, ctypes.POINTER(vp)]
         L.fm_batch_run.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(BatchStats)]
+        L.fm_batch_set_engine.argtypes = [vp, i32]
         L.fm_batch_rows.argtypes = [vp, u32, ctypes.POINTER(vp), ctypes.POINTER(u64)]
         L.fm_batch_copy_rows.argtypes = [vp, u32, vp, u64, ctypes.POINTER(u64)]
         L.fm_batch_copy_tables.argtypes = [vp, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]
@@ -314,13 +322,16 @@ class PinnedRows:
 
 def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_rows=None, roots=None,
           profile=False, stream=None, allow_truncation=False, order=ORDER_AUTO, host_direct=False, work_limit=0,
-          allow_limit=False):
+          allow_limit=False, engine=ENGINE_PERSISTENT, wait_limit_ms=0, test_stall_barrier=False,
+          allow_device_error=False):
     """Run fm_match.  Returns the Result struct; with ``host_rows`` (a
     PinnedRows or a C-contiguous uint32 numpy array) the table is copied there.
     ``host_direct`` (PinnedRows only): the kernels write the table straight
     into the pinned host buffer instead of device memory.  ``work_limit``:
     stop after that many embeddings or partial matches (FM_ERR_LIMIT, raised
-    unless ``allow_limit``)."""
+    unless ``allow_limit``).  ``engine``: ENGINE_PERSISTENT (one cooperative
+    launch, passes scheduled on the device) or ENGINE_LEVELS (launch pairs per
+    pass, drains scheduled by the host)."""
     o = MatchOpts()
     lib().fm_match_opts_default(ctypes.byref(o))
     o.mode = mode
@@ -329,6 +340,9 @@ def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_ro
     o.order = order
     o.host_direct = 1 if host_direct else 0
     o.work_limit = int(work_limit)
+    o.engine = int(engine)
+    o.wait_limit_ms = int(wait_limit_ms)
+    o.test_stall_barrier = 1 if test_stall_barrier else 0
     if stream is not None:
         o.stream = stream
     if roots is not None:
@@ -342,7 +356,8 @@ def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_ro
             o.host_rows_cap = host_rows.size // max(1, query.q)
     r = Result()
     st = lib().fm_match(ctx._h, graph._h, query._h, ctypes.byref(o), ctypes.byref(r))
-    allow = ((FM_ERR_OUTPUT_OVERFLOW,) if allow_truncation else ()) + ((FM_ERR_LIMIT,) if allow_limit else ())
+    allow = ((FM_ERR_OUTPUT_OVERFLOW,) if allow_truncation else ()) + ((FM_ERR_LIMIT,) if allow_limit else ()) + \
+        ((FM_ERR_DEVICE,) if allow_device_error else ())
     _check(st, "fm_match", allow=allow)
     r.status = st
     return r
@@ -388,6 +403,9 @@ class Batch:
             ptr, cap = host.ctypes.data, host.size
         _check(lib().fm_batch_copy_tables(self._h, ptr, cap, offs, ctypes.byref(words)), "fm_batch_copy_tables")
         return words.value, [None if offs[i] == (1 << 64) - 1 else int(offs[i]) for i in range(n)]
+
+    def set_engine(self, engine):
+        _check(lib().fm_batch_set_engine(self._h, int(engine)), "fm_batch_set_engine")
 
     def tune(self):
         st = BatchStats()

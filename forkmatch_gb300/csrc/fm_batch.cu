@@ -52,13 +52,17 @@ struct BatchParams {
     const uint32_t* heads;                    // per-label root lists of the graph
     uint32_t depth;
     uint32_t kmax;                            // segment records per parent reserved in shared memory
-    // work items
+    // work items (deferred rings as in ExpandParams: def_in[(def_in_pos + i) %
+    // def_cap], new deferrals at def_out_pos while fewer than def_room)
     const uint32_t* def_in;
     uint32_t ndef_in;
     uint64_t fresh_base;
     uint64_t n_items;
     uint32_t* def_out;
     uint32_t def_cap;
+    uint64_t def_in_pos;
+    uint64_t def_out_pos;
+    uint32_t def_room;
     // outputs: next level (columns 0..d, query id in column d+1), per-query results
     uint32_t* pout;
     uint64_t ocap;
@@ -290,18 +294,19 @@ __device__ __forceinline__ void bprocess(const BatchParams& P, const BMem& m, ui
 }
 
 __device__ __forceinline__ uint32_t bitem_chunk(const BatchParams& P, unsigned long long item) {
-    return item < P.ndef_in ? P.def_in[item] : (uint32_t)(P.fresh_base + (item - P.ndef_in));
+    return item < P.ndef_in ? P.def_in[(P.def_in_pos + item) % P.def_cap]
+                            : (uint32_t)(P.fresh_base + (item - P.ndef_in));
 }
 
 __device__ __forceinline__ void bdefer(const BatchParams& P, uint32_t chunk) {
     const unsigned idx = atomicAdd(&P.ctl->ndef, 1u);
-    if (idx < P.def_cap) P.def_out[idx] = chunk;
+    const uint32_t room = P.def_room ? P.def_room : P.def_cap;
+    if (idx < room) P.def_out[(P.def_out_pos + idx) % P.def_cap] = chunk;
     else atomicOr(&P.ctl->error, 1u);
 }
 
 template <bool ROOTS>
-__global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand(const __grid_constant__ BatchParams P) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void bexpand_main(const BatchParams& P, unsigned char* smem_raw) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t d = P.depth;
     const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax);
@@ -389,9 +394,8 @@ __global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand(const __grid_consta
 }
 
 template <bool ROOTS>
-__global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand_heavy(const __grid_constant__ BatchParams P) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const unsigned long long h = P.ctl->heavy;
+__device__ __forceinline__ void bexpand_heavy(const BatchParams& P, unsigned char* smem_raw) {
+    const unsigned long long h = *(volatile unsigned long long*)&P.ctl->heavy;
     const uint32_t nent = (uint32_t)(h >> 32);
     const uint32_t npieces = (uint32_t)h;
     if (nent == 0) return;
@@ -423,6 +427,117 @@ __global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand_heavy(const __grid_
         bprocess<ROOTS>(P, m, e.chunk, begin, end, lane, d, nst);
     }
     if (nst) bflush<ROOTS>(P, m, nst, lane, d, last_chunk);
+}
+
+template <bool ROOTS>
+__global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand(const __grid_constant__ BatchParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bexpand_main<ROOTS>(P, smem_raw);
+}
+
+template <bool ROOTS>
+__global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand_heavy(const __grid_constant__ BatchParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bexpand_heavy<ROOTS>(P, smem_raw);
+}
+
+// Persistent batch engine: one cooperative launch runs every level pass of
+// the whole batch, scheduled on the device exactly like the single-query
+// persistent kernel (fm_match.cu): per-depth work queues (deferred ring, then
+// fresh chunks), depth-first drains, bounded grid barriers.
+struct BatchPersistArgs {
+    SchedState* sched;
+    uint32_t* levels[kMaxQ];
+    uint32_t kmax[kMaxQ];
+    uint32_t* rings;
+    uint32_t ring_cap;
+    uint32_t maxq;
+    int hold_first_barrier;
+};
+
+__global__ void __launch_bounds__(kBWarps * 32, 5) k_bpersist(const __grid_constant__ BatchParams P0,
+                                                              const __grid_constant__ BatchPersistArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(16) BatchParams P;
+    __shared__ unsigned flag_s, cur_s;
+    SchedState* S = A.sched;
+    {
+        const uint32_t* src = (const uint32_t*)&P0;
+        uint32_t* dst = (uint32_t*)&P;
+        for (uint32_t i = threadIdx.x; i < sizeof(BatchParams) / 4; i += blockDim.x) dst[i] = src[i];
+    }
+    bool first = true;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned d = *(volatile unsigned*)&S->cur;
+            if (*(volatile unsigned*)&S->error) d = 0;
+            cur_s = d;
+            if (d) {
+                const volatile SchedLevel* L = &S->lv[d];
+                const unsigned long long ring = L->tail - L->head;
+                const unsigned long long n_chunks = (L->n_parents + 31) / 32;
+                P.depth = d;
+                P.kmax = A.kmax[d];
+                P.pin = d == 1 ? nullptr : A.levels[d];
+                P.pout = d + 1 < A.maxq ? A.levels[d + 1] : nullptr;
+                P.n_parents = L->n_parents;
+                P.ndef_in = (uint32_t)ring;
+                P.fresh_base = L->fresh;
+                P.n_items = ring + (n_chunks - L->fresh);
+                P.def_in = A.rings + (uint64_t)d * A.ring_cap;
+                P.def_out = A.rings + (uint64_t)d * A.ring_cap;
+                P.def_cap = A.ring_cap;
+                P.def_in_pos = L->head;
+                P.def_out_pos = L->tail;
+                P.def_room = A.ring_cap - (uint32_t)ring;
+                P.ctl = P0.ctl + d;
+            }
+        }
+        __syncthreads();
+        const unsigned d = cur_s;
+        if (d == 0) break;
+        if (d == 1) bexpand_main<true>(P, smem_raw);
+        else bexpand_main<false>(P, smem_raw);
+        if (!dev::grid_barrier(S, first && A.hold_first_barrier && blockIdx.x == 0, &flag_s)) break;
+        first = false;
+        if (d == 1) bexpand_heavy<true>(P, smem_raw);
+        else bexpand_heavy<false>(P, smem_raw);
+        if (!dev::grid_barrier(S, false, &flag_s)) break;
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            dev::sched_advance(S, P0.ctl, d, d + 1 < A.maxq, P.n_items, P.ndef_in, P.def_room, false);
+        if (!dev::grid_barrier(S, false, &flag_s)) break;
+    }
+}
+
+int bpersist_blocks_per_sm(size_t smem) {
+    allow_dynamic_smem((const void*)&k_bpersist);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)&k_bpersist, kBWarps * 32, smem) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    return n;
+}
+
+cudaError_t launch_bpersist(const BatchParams& p, const BatchPersistArgs& a, int grid, size_t smem,
+                            cudaStream_t s) {
+    BatchParams q = p;
+    q.max_warps = (uint32_t)grid * kBWarps;
+    q.n_parents_dev = nullptr;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kBWarps * 32);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void* args[] = {(void*)&q, (void*)&a};
+    return cudaLaunchKernelExC(&cfg, (const void*)&k_bpersist, args);
 }
 
 cudaError_t launch_batch_level(const BatchParams& p, bool roots, int grid, int heavy_grid, size_t smem,
@@ -484,6 +599,22 @@ struct fm_batch {
     }
     uint32_t piece_shift = 0;
     uint32_t sm_fraction = 4;             // quarters of the full grid used by the main pass
+    bool persistent = true;               // one cooperative launch per run (else level launches)
+    bool graph_ok = true;                 // capture of the run succeeded (else launched directly)
+    uint64_t cap_full = 0;                // largest level buffer (rows) SOLN_PREALLOC allows
+    uint64_t cap_floor = 0;               // smallest level buffer one chunk per level needs
+    uint32_t bank_shift = 0;              // tuned: level buffers of cap_full >> bank_shift rows
+    char* soln = nullptr;
+
+    // Level buffers of `cap` rows each, packed from the start of the level region.
+    void layout_levels(uint64_t cap) {
+        level_cap = cap;
+        uint64_t loff = 0;
+        for (uint32_t d = 2; d < maxq; d++) {
+            level[d] = (uint32_t*)(soln + loff);
+            loff += 4ull * (d + 1) * cap;
+        }
+    }
     std::vector<uint64_t> counts;
     std::vector<uint64_t> single_counts;
     uint64_t launches = 0;
@@ -553,6 +684,91 @@ struct BatchRun {
     // occupancy queries and attribute changes happen here, before any capture
     void prepare() {
         for (uint32_t d = 1; d < b->maxq; d++) gfull[d] = cv.sms * batch_blocks_per_sm(d == 1, smem(d));
+        pgrid = 0;
+        if (b->persistent) {
+            const int per_sm = bpersist_blocks_per_sm(psmem());
+            if (per_sm > 0) pgrid = cv.sms * std::max(1, (per_sm * (int)b->sm_fraction + 3) / 4);
+        }
+    }
+    int pgrid = 0;                        // persistent grid (0: level launches)
+    size_t psmem() const {
+        size_t m = 0;
+        for (uint32_t d = 1; d < b->maxq; d++) m = std::max<size_t>(m, bper_warp_bytes(d, b->kmax[d]));
+        return m * kBWarps;
+    }
+
+    // The persistent run as stream work (what the CUDA graph captures): clear
+    // the per-query results and control blocks, write the initial schedule,
+    // one cooperative launch, read back the schedule and the per-query results.
+    fm_status enqueue_persist() {
+        FM_CUDA(cudaMemsetAsync(b->d_qpos, 0, nq * sizeof(unsigned long long), s));
+        FM_CUDA(cudaMemsetAsync(cv.ctl, 0, b->maxq * sizeof(LaunchCtl), s));
+        FM_CUDA(launch_sched_init(cv.sched, b->maxq, (unsigned long long)nq * base.chunks_per_query * 32, 0,
+                                  60000ull * 1000000ull, s));
+        BatchParams p = base;
+        p.pstride = b->level_cap;
+        p.ocap = b->level_cap;
+        p.ctl = cv.ctl;
+        BatchPersistArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.sched = cv.sched;
+        for (uint32_t d = 0; d < (uint32_t)kMaxQ; d++) {
+            a.levels[d] = b->level[d];
+            a.kmax[d] = b->kmax[d];
+        }
+        a.rings = cv.defs;
+        a.ring_cap = 2 * cv.def_cap;
+        a.maxq = b->maxq;
+        FM_CUDA(launch_bpersist(p, a, pgrid, psmem(), s));
+        FM_CUDA(cudaMemcpyAsync(cv.h_sched, cv.sched, sizeof(SchedState), cudaMemcpyDeviceToHost, s));
+        FM_CUDA(cudaMemcpyAsync(b->h_qpos, b->d_qpos, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        return FM_OK;
+    }
+
+    fm_status run_persist(bool use_graph) {
+        bool ran = false;
+        if (use_graph && b->graph_ok) {
+            cudaGraphExec_t& exec = b->exec[base.table_mode ? 1 : 0];
+            if (!exec) {
+                cudaGraph_t graph = nullptr;
+                FM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                fm_status st = enqueue_persist();
+                cudaError_t e = cudaStreamEndCapture(s, &graph);
+                if (st == FM_OK && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+                if (graph) cudaGraphDestroy(graph);
+                if (st != FM_OK || e != cudaSuccess) {
+                    // a cooperative launch this toolkit cannot capture: run it directly
+                    cudaGetLastError();
+                    exec = nullptr;
+                    b->graph_ok = false;
+                }
+            }
+            if (exec) {
+                FM_CUDA(cudaGraphLaunch(exec, s));
+                ran = true;
+            }
+        }
+        if (!ran) FM_TRY(enqueue_persist());
+        FM_CUDA(cudaStreamSynchronize(s));
+        b->launches += 2;   // the schedule initialisation and the persistent kernel
+        const SchedState& h = *cv.h_sched;
+        if (h.error & kSchedErrWait) {
+            set_error("a grid-wide wait of the persistent batch kernel ran out");
+            return FM_ERR_DEVICE;
+        }
+        if (h.error & kSchedErrPasses) {
+            set_error("the persistent schedule exceeded its pass bound");
+            return FM_ERR_DEVICE;
+        }
+        if (h.error & kSchedErrRing) {
+            set_error("deferred-chunk ring overflow");
+            return FM_ERR_DEVICE;
+        }
+        if (h.error & kSchedErrPool) {
+            set_error("one 32-parent chunk needs more rows than a level buffer holds; raise SOLN_PREALLOC");
+            return FM_ERR_POOL;
+        }
+        return FM_OK;
     }
     int full_grid(uint32_t d) const { return gfull[d]; }
     int main_grid(uint32_t d) const { return std::max(1, full_grid(d) * (int)b->sm_fraction / 4); }
@@ -647,6 +863,7 @@ struct BatchRun {
 
     fm_status run(bool use_graph) {
         prepare();
+        if (pgrid > 0) return run_persist(use_graph);
         if (use_graph) {
             cudaGraphExec_t& exec = b->exec[base.table_mode ? 1 : 0];
             if (!exec) {
@@ -773,12 +990,10 @@ fm_status batch_create_impl(fm_context* ctx, const fm_graph* graph, const fm_que
             set_error("SOLN_PREALLOC cannot hold one 32-parent chunk per level for this graph");
             return FM_ERR_POOL;
         }
-        b->level_cap = cap;
-        uint64_t loff = 0;
-        for (uint32_t d = 2; d < b->maxq; d++) {
-            b->level[d] = (uint32_t*)(cv.soln + loff);
-            loff += 4ull * (d + 1) * cap;
-        }
+        b->soln = cv.soln;
+        b->cap_full = cap;
+        b->cap_floor = (uint64_t)g.max_len * 32 + 32;
+        b->layout_levels(cap);
         b->h_plans = plans;
         if (scr) {
             // caller-owned scratch: no allocation (a server must not call
@@ -923,6 +1138,9 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
         stats->single_queries = (uint32_t)b->single.size();
         stats->piece_shift = b->piece_shift;
         stats->grid_quarters = b->sm_fraction;
+        stats->level_rows = b->level_cap;
+        stats->persistent = b->persistent ? 1 : 0;
+        stats->graph = (b->replay && b->graph_ok) ? 1 : 0;
         for (uint32_t i = 0; i < b->n; i++) stats->embeddings += b->counts[i];
     }
     if (truncated) {
@@ -967,7 +1185,12 @@ fm_status fm_batch_copy_rows(const fm_batch* b, uint32_t i, uint32_t* host, uint
 }  // extern "C"
 
 void fm::batch_set_replay(fm_batch* b, bool replay) {
-    if (b) b->replay = replay;
+    // a server's batches run once, beside other slots' work: no capture, and
+    // level launches (a cooperative launch needs the whole GPU resident)
+    if (b) {
+        b->replay = replay;
+        if (!replay) b->persistent = false;
+    }
 }
 
 extern "C" {
@@ -1002,40 +1225,66 @@ fm_status fm_batch_copy_tables(const fm_batch* b, uint32_t* host, uint64_t cap_w
     return FM_OK;
 }
 
+fm_status fm_batch_set_engine(fm_batch* b, int32_t engine) {
+    if (!b || (engine != FM_ENGINE_PERSISTENT && engine != FM_ENGINE_LEVELS)) return FM_ERR_ARG;
+    if (!b->replay && engine == FM_ENGINE_PERSISTENT) {
+        set_error("a server's batches use level launches");
+        return FM_ERR_ARG;
+    }
+    b->persistent = engine == FM_ENGINE_PERSISTENT;
+    b->drop_graphs();
+    return FM_OK;
+}
+
 fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
     if (!b) return FM_ERR_ARG;
-    // Search the split granularity (heavy piece size, the intersection tile a
-    // warp walks) and the grid of the main pass (warps in flight per query
-    // level); keep the fastest.  Each configuration runs the whole batch.
-    const uint32_t shifts[] = {0, 1, 2};
+    // Search the split granularity (heavy piece size: the intersection tile a
+    // warp walks), the grid (warps in flight per SM) and the level-buffer
+    // size (rows per buffer, the bank size: small buffers keep the rows of a
+    // depth-first drain in L2, large ones need fewer passes); keep the
+    // fastest.  Each configuration runs the whole batch twice (capture, then
+    // the timed replay).
+    const uint32_t shifts[] = {0, 1};
     const uint32_t quarters[] = {2, 4};
+    const uint32_t banks[] = {0, 4, 8};
     double best_ms = -1;
-    uint32_t bs = b->piece_shift, bq = b->sm_fraction;
-    for (uint32_t sh : shifts) {
-        for (uint32_t qu : quarters) {
-            b->piece_shift = sh;
-            b->sm_fraction = qu;
-            b->drop_graphs();
-            fm_batch_stats st;
-            fm_status s = fm_batch_run(b, nullptr, &st);   // builds the graph
-            if (s != FM_OK && s != FM_ERR_OUTPUT_OVERFLOW) return s;
-            s = fm_batch_run(b, nullptr, &st);             // timed replay
-            if (s != FM_OK && s != FM_ERR_OUTPUT_OVERFLOW) return s;
-            if (best_ms < 0 || st.wall_ms < best_ms) {
-                best_ms = st.wall_ms;
-                bs = sh;
-                bq = qu;
+    uint32_t bs = b->piece_shift, bq = b->sm_fraction, bb = b->bank_shift;
+    for (uint32_t bank : banks) {
+        if (bank && (b->cap_full >> bank) < b->cap_floor) continue;
+        for (uint32_t sh : shifts) {
+            for (uint32_t qu : quarters) {
+                b->piece_shift = sh;
+                b->sm_fraction = qu;
+                b->bank_shift = bank;
+                b->layout_levels(b->cap_full >> bank);
+                b->drop_graphs();
+                fm_batch_stats st;
+                fm_status s = fm_batch_run(b, nullptr, &st);   // builds the graph
+                if (s != FM_OK && s != FM_ERR_OUTPUT_OVERFLOW) return s;
+                s = fm_batch_run(b, nullptr, &st);             // timed replay
+                if (s != FM_OK && s != FM_ERR_OUTPUT_OVERFLOW) return s;
+                if (best_ms < 0 || st.wall_ms < best_ms) {
+                    best_ms = st.wall_ms;
+                    bs = sh;
+                    bq = qu;
+                    bb = bank;
+                }
             }
         }
     }
     b->piece_shift = bs;
     b->sm_fraction = bq;
+    b->bank_shift = bb;
+    b->layout_levels(b->cap_full >> bb);
     b->drop_graphs();
     if (best) {
         std::memset(best, 0, sizeof(*best));
         best->wall_ms = best_ms;
         best->piece_shift = bs;
         best->grid_quarters = bq;
+        best->level_rows = b->level_cap;
+        best->persistent = b->persistent ? 1 : 0;
+        best->graph = b->graph_ok ? 1 : 0;
     }
     return FM_OK;
 }

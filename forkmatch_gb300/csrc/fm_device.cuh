@@ -82,5 +82,119 @@ __device__ __forceinline__ void slot_locate(uint32_t s, const uint32_t* excl_s, 
     t = s - excl_s[j];
 }
 
+// ------------------------------------------------------- persistent engine
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid-wide barrier of a cooperative launch (every block of the grid is
+// resident).  One thread per block arrives; the last arrival resets the count
+// and advances the generation.  Every wait is bounded: a wait that exceeds
+// S->wait_limit_ns raises kSchedErrWait, and a wait ends early once any error
+// bit is set.  Returns false in every thread of the block when an error bit is
+// set.  `skip_arrive` (tests only) makes this block wait without arriving, so
+// that every wait of this barrier runs out.
+__device__ __forceinline__ bool grid_barrier(SchedState* S, bool skip_arrive, unsigned* flag_s) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = &S->bar_gen;
+        volatile unsigned* err = &S->error;
+        const unsigned g = *gen;
+        __threadfence();
+        bool released = false;
+        if (!skip_arrive) {
+            const unsigned arrived = atomicAdd(&S->bar_count, 1u) + 1u;
+            if (arrived == gridDim.x) {
+                atomicExch(&S->bar_count, 0u);
+                __threadfence();
+                atomicAdd(&S->bar_gen, 1u);
+                released = true;
+            }
+        }
+        if (!released) {
+            const unsigned long long t0 = global_ns();
+            unsigned long long dt = 0;
+            while (*gen == g && *err == 0) {
+                dt = global_ns() - t0;
+                if (dt > S->wait_limit_ns) {
+                    atomicOr(&S->error, kSchedErrWait);
+                    break;
+                }
+                __nanosleep(200);
+            }
+            if (dt > 0) atomicMax(&S->wait_seen_ns, dt);
+        }
+        __threadfence();
+        *flag_s = *err;
+    }
+    __syncthreads();
+    return *(volatile unsigned*)flag_s == 0;
+}
+
+// Chunks of depth d that no pass has consumed yet (deferred or fresh).
+__device__ __forceinline__ unsigned long long sched_remaining(const SchedState* S, unsigned d) {
+    const volatile SchedLevel* L = &S->lv[d];
+    return (L->tail - L->head) + ((L->n_parents + 31) / 32 - L->fresh);
+}
+
+// The schedule step after a pass of depth d (one thread): account the pass's
+// claims (consumed deferred entries leave the ring head, new deferrals were
+// appended at its tail), then pick the next pass depth first -- descend into
+// the level the pass just filled, else repeat d while it has chunks left,
+// else return to the deepest ancestor with chunks left; 0 ends the match.
+// `mid`: the pass wrote a next level.  `items`, `ring_count`, `def_room`: the
+// pass's work items, deferred items among them and room for new deferrals.
+__device__ __forceinline__ void sched_advance(SchedState* S, LaunchCtl* ctl_base, unsigned d, bool mid,
+                                              unsigned long long items, unsigned long long ring_count,
+                                              unsigned long long def_room, bool limit_hit) {
+    volatile LaunchCtl* c = ctl_base + d;
+    SchedLevel* L = &S->lv[d];
+    const unsigned long long claimed = c->claim < items ? c->claim : items;
+    const unsigned long long ring_claimed = claimed < ring_count ? claimed : ring_count;
+    const unsigned long long ndef = c->ndef;
+    L->head += ring_claimed;
+    L->tail += ndef;
+    L->fresh += claimed - ring_claimed;
+    L->parents += c->parents;
+    L->lookups += c->lookups;
+    L->list_words += c->list_words;
+    L->passes += 1;
+    S->passes += 1;
+    const unsigned long long produced = mid ? c->produced : 0;
+    L->produced += produced;
+    S->produced_total += produced;
+    unsigned err = 0;
+    if (c->error || ndef > def_room) err |= kSchedErrRing;
+    const unsigned long long left = sched_remaining(S, d);
+    if (mid && produced == 0 && left == items && items > 0) err |= kSchedErrPool;
+    if (limit_hit || (S->work_limit && S->produced_total > S->work_limit)) err |= kSchedErrLimit;
+    if (S->passes > kSchedMaxPasses) err |= kSchedErrPasses;
+    unsigned next = 0;
+    if (!err) {
+        if (mid && produced > 0) {
+            next = d + 1;
+            SchedLevel* N = &S->lv[next];
+            N->n_parents = produced;
+            N->fresh = 0;
+            N->head = 0;
+            N->tail = 0;
+        } else {
+            next = d;
+            while (next >= 1 && sched_remaining(S, next) == 0) next--;
+        }
+    }
+    if (next) {
+        unsigned long long* w = (unsigned long long*)(ctl_base + next);
+        for (unsigned i = 0; i < sizeof(LaunchCtl) / 8; i++) w[i] = 0;
+    }
+    if (err) atomicOr(&S->error, err);
+    __threadfence();
+    *(volatile unsigned*)&S->cur = next;
+    __threadfence();
+}
+
 }  // namespace dev
 }  // namespace fm

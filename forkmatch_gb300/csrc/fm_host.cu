@@ -52,8 +52,10 @@ struct fm_context {
     uint32_t def_cap = 0;
     HeavyEntry* heavy = nullptr;  // heavy-chunk entries of the current launch
     uint32_t heavy_cap = 0;
+    SchedState* sched = nullptr;  // persistent engine schedule (device)
     LaunchCtl* h_ctl = nullptr; // pinned mirrors
     MatchTotals* h_tot = nullptr;
+    SchedState* h_sched = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> prof;
     bool serving = false;       // a server owns the slab (fm_match/fm_batch refuse)
@@ -69,12 +71,16 @@ uint64_t env_u64(const char* name, uint64_t dflt) {
     return (end && *end == 0) ? (uint64_t)x : dflt;
 }
 
-// [0, 4 KiB) control blocks, [4 KiB, 48 MiB) deferred-chunk lists (two per
-// depth), [48 MiB, 64 MiB) heavy-chunk entries
+// [0, 4 KiB) control blocks, [4 KiB, 8 KiB) match totals and the persistent
+// schedule, [8 KiB, 48 MiB) deferred-chunk lists (two per depth, which the
+// persistent engine uses as one ring per depth), [48 MiB, 64 MiB) heavy-chunk
+// entries
 void set_misc(fm_context* c, char* misc) {
     static_assert(kMaxQ * sizeof(LaunchCtl) <= 4096, "per-level control blocks must fit in 4 KiB");
+    static_assert(256 + sizeof(SchedState) <= 4096, "totals and schedule must fit in 4 KiB");
     c->ctl = (LaunchCtl*)misc;                 // one control block per depth
     c->tot = (MatchTotals*)(misc + 4096);
+    c->sched = (SchedState*)(misc + 4096 + 256);
     c->defs = (uint32_t*)(misc + 8192);
     c->def_cap = (uint32_t)(((48ull << 20) - 8192) / 4 / (2 * kMaxQ));
     c->heavy = (HeavyEntry*)(misc + (48ull << 20));
@@ -160,6 +166,7 @@ void fm_context_destroy(fm_context* c) {
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
     if (c->h_tot) cudaFreeHost(c->h_tot);
+    if (c->h_sched) cudaFreeHost(c->h_sched);
     if (c->slab) cudaFree(c->slab);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -199,6 +206,7 @@ fm_status fm_context_create(const fm_knobs* knobs, fm_context** out) {
     set_misc(c.get(), c->slab + ((k.prealloc_bytes - kMiscBytes) & ~255ull));
     FM_CUDA(cudaHostAlloc(&c->h_ctl, kMaxQ * sizeof(LaunchCtl), cudaHostAllocDefault));
     FM_CUDA(cudaHostAlloc(&c->h_tot, sizeof(MatchTotals), cudaHostAllocDefault));
+    FM_CUDA(cudaHostAlloc(&c->h_sched, sizeof(SchedState), cudaHostAllocDefault));
     FM_CUDA(cudaEventCreate(&c->ev0));
     FM_CUDA(cudaEventCreate(&c->ev1));
     *out = c.release();
@@ -490,6 +498,7 @@ struct MatchRun {
         fm_level_stats& ls = res->level[d];
         ls.launches++;
         res->launches++;
+        res->passes++;
         ls.parents += c.parents;
         ls.lookups += c.lookups;
         ls.list_words += c.list_words;
@@ -566,6 +575,68 @@ struct MatchRun {
             fm_status st = drain_level(d, n_parents[d], d == 1, c.ndef, claimed, def_list(d, 1), def_list(d, 0));
             if (st != FM_OK) return st;
         }
+        return FM_OK;
+    }
+
+    // Persistent engine: one cooperative launch runs every pass; the device
+    // schedules them (depth first over levels whose buffer filled) from the
+    // per-depth work queues.  Returns FM_ERR_UNSUPPORTED (nothing launched)
+    // when no block of the kernel fits an SM with this plan's shared memory.
+    fm_status run_persistent(uint64_t n_roots, const fm_match_opts& opts) {
+        const uint32_t q = plan->q;
+        const int last_mode = table ? kModeLastTable : kModeLastCount;
+        const size_t smem = persist_smem_bytes(base.plan, nreq_depth);
+        const int per_sm = persist_blocks_per_sm(last_mode, dups, smem);
+        if (per_sm < 1) return FM_ERR_UNSUPPORTED;
+        const int grid = ctx->sms * per_sm;
+        SchedState& h = *ctx->h_sched;
+        const unsigned long long wait_ns =
+            (unsigned long long)(opts.wait_limit_ms ? opts.wait_limit_ms : 60000u) * 1000000ull;
+        FM_CUDA(launch_sched_init(ctx->sched, q, n_roots, work_limit, wait_ns, s));
+        FM_CUDA(cudaMemsetAsync(ctx->ctl, 0, q * sizeof(LaunchCtl), s));
+        PersistArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.sched = ctx->sched;
+        for (uint32_t d = 0; d < (uint32_t)kMaxQ; d++) a.levels[d] = level[d];
+        a.rings = ctx->defs;
+        a.ring_cap = 2 * ctx->def_cap;
+        a.n_roots = n_roots;
+        a.hold_first_barrier = opts.test_stall_barrier ? 1 : 0;
+        ExpandParams p = base;
+        p.pstride = level_cap;
+        p.ocap = level_cap;
+        p.ctl = ctx->ctl;
+        FM_CUDA(launch_persist(p, a, last_mode, dups, grid, smem, s));
+        FM_CUDA(cudaMemcpyAsync(&h, ctx->sched, sizeof(h), cudaMemcpyDeviceToHost, s));
+        FM_CUDA(cudaStreamSynchronize(s));
+        for (uint32_t d = 1; d < q; d++) {
+            fm_level_stats& ls = res->level[d];
+            ls.parents += h.lv[d].parents;
+            ls.lookups += h.lv[d].lookups;
+            ls.list_words += h.lv[d].list_words;
+            ls.produced += h.lv[d].produced;
+            ls.launches += (uint32_t)h.lv[d].passes;
+        }
+        res->launches += 1;
+        res->passes += (uint32_t)h.passes;
+        res->max_wait_ns = h.wait_seen_ns;
+        if (h.error & kSchedErrWait) {
+            set_error("a grid-wide wait of the persistent kernel ran out (wait_limit_ms)");
+            return FM_ERR_DEVICE;
+        }
+        if (h.error & kSchedErrPasses) {
+            set_error("the persistent schedule exceeded its pass bound");
+            return FM_ERR_DEVICE;
+        }
+        if (h.error & kSchedErrRing) {
+            set_error("deferred-chunk ring overflow");
+            return FM_ERR_DEVICE;
+        }
+        if (h.error & kSchedErrPool) {
+            set_error("one 32-parent chunk needs more rows than a level buffer holds; raise SOLN_PREALLOC");
+            return FM_ERR_POOL;
+        }
+        if (h.error & kSchedErrLimit) return FM_ERR_LIMIT;
         return FM_OK;
     }
 
@@ -818,7 +889,13 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         b.heavy_cap = ctx->heavy_cap;
         b.work_limit = opts.work_limit;
         run.work_limit = opts.work_limit;
-        fm_status st = run.run(n_roots);
+        fm_status st = FM_ERR_UNSUPPORTED;
+        out->engine = FM_ENGINE_LEVELS;
+        if (opts.engine == FM_ENGINE_PERSISTENT && !opts.profile) {
+            st = run.run_persistent(n_roots, opts);
+            if (st != FM_ERR_UNSUPPORTED) out->engine = FM_ENGINE_PERSISTENT;
+        }
+        if (st == FM_ERR_UNSUPPORTED) st = run.run(n_roots);
         if (st == FM_ERR_LIMIT) limited = true;
         else if (st != FM_OK) return st;
     }
@@ -865,6 +942,7 @@ fm_status fm::context_create_view(fm_context* owner, char* misc, fm_context** ou
     set_misc(c.get(), misc);
     FM_CUDA(cudaHostAlloc(&c->h_ctl, kMaxQ * sizeof(LaunchCtl), cudaHostAllocDefault));
     FM_CUDA(cudaHostAlloc(&c->h_tot, sizeof(MatchTotals), cudaHostAllocDefault));
+    FM_CUDA(cudaHostAlloc(&c->h_sched, sizeof(SchedState), cudaHostAllocDefault));
     FM_CUDA(cudaEventCreate(&c->ev0));
     FM_CUDA(cudaEventCreate(&c->ev1));
     *out = c.release();
@@ -906,5 +984,7 @@ fm::ContextView fm::context_view(fm_context* c) {
     v.def_cap = c->def_cap;
     v.heavy = c->heavy;
     v.heavy_cap = c->heavy_cap;
+    v.sched = c->sched;
+    v.h_sched = c->h_sched;
     return v;
 }

@@ -158,13 +158,21 @@ struct ExpandParams {
     uint32_t root_begin;            // roots: parent p is vertex root_begin + p
     const uint32_t* root_list;      // roots, when set: parent p is vertex root_list[p]
     uint32_t depth;                 // parent rows have `depth` entries; new vertex goes to column depth
-    // work items
+    // work items: ndef_in deferred chunks, then fresh chunks from fresh_base.
+    // Deferred lists are rings of def_cap entries: deferred item i is
+    // def_in[(def_in_pos + i) % def_cap]; a new deferral goes to
+    // def_out[(def_out_pos + k) % def_cap] while k < def_room.  The level-launch
+    // driver uses two plain lists (positions 0, room def_cap); the persistent
+    // kernel keeps one ring per depth (def_in == def_out).
     const uint32_t* def_in;
     uint32_t ndef_in;
     uint64_t fresh_base;            // first fresh chunk
     uint64_t n_items;               // ndef_in + fresh chunks
     uint32_t* def_out;
     uint32_t def_cap;
+    uint64_t def_in_pos;
+    uint64_t def_out_pos;
+    uint32_t def_room;
     // outputs
     uint32_t* pout;                 // SoA, column c at pout + c*ocap
     uint64_t ocap;
@@ -181,6 +189,58 @@ struct ExpandParams {
     unsigned long long work_limit;
 };
 constexpr unsigned int kLimitFlag = 2u;
+
+// ------------------------------------------------------- persistent engine
+// One cooperative launch runs every level pass of a match: each pass is the
+// main pass, a grid barrier, the heavy pass, a grid barrier, then block 0
+// advances the schedule (depth-first over levels whose output buffer filled)
+// and a last barrier publishes it.  Every barrier wait is bounded in time.
+struct SchedLevel {                   // per depth, device memory
+    unsigned long long n_parents;     // rows of this level (roots at depth 1)
+    unsigned long long fresh;         // fresh chunks consumed
+    unsigned long long head, tail;    // deferred-chunk ring positions
+    unsigned long long parents, lookups, list_words, produced, passes;
+};
+
+constexpr unsigned kSchedErrRing = 1u;       // a deferred-chunk ring overflowed
+constexpr unsigned kSchedErrPool = 2u;       // a chunk needs more rows than a level buffer holds
+constexpr unsigned kSchedErrWait = 4u;       // a grid barrier wait ran out of time
+constexpr unsigned kSchedErrLimit = 8u;      // work limit (partial matches produced) reached
+constexpr unsigned kSchedErrPasses = 16u;    // more passes than any match can need (a schedule defect)
+constexpr unsigned long long kSchedMaxPasses = 1ull << 26;
+
+struct SchedState {
+    unsigned int cur;                 // depth of the next pass; 0 = finished
+    unsigned int error;               // kSchedErr* bits
+    unsigned int bar_count, bar_gen;  // grid barrier
+    unsigned int q;                   // levels 1 .. q-1
+    unsigned int pad[3];
+    unsigned long long passes;
+    unsigned long long produced_total;
+    unsigned long long work_limit;    // partial matches; 0 = none
+    unsigned long long wait_limit_ns; // bound on one barrier wait
+    unsigned long long wait_seen_ns;  // longest barrier wait seen
+    SchedLevel lv[kMaxQ];
+};
+
+// Per-match constants of the persistent engine that ExpandParams does not hold.
+struct PersistArgs {
+    SchedState* sched;
+    uint32_t* levels[kMaxQ];          // level buffer of depth d (rows of d entries), d >= 2
+    uint32_t* rings;                  // one deferred ring of ring_cap entries per depth
+    uint32_t ring_cap;
+    uint64_t n_roots;
+    int hold_first_barrier;           // tests: block 0 skips the first barrier
+};
+
+// Dynamic shared memory and grid of the persistent kernel for a plan.
+size_t persist_smem_bytes(const DevPlan& plan, const uint32_t* nreq_depth);
+int persist_blocks_per_sm(int last_mode, bool dups, size_t smem);
+cudaError_t launch_persist(const ExpandParams& p, const PersistArgs& a, int last_mode, bool dups, int grid,
+                           size_t smem, cudaStream_t s);
+// Writes the initial schedule (depth 1, n_roots rows) with a one-block kernel.
+cudaError_t launch_sched_init(SchedState* S, unsigned q, unsigned long long n_roots, unsigned long long work_limit,
+                              unsigned long long wait_ns, cudaStream_t s);
 
 // Launch one level expansion: the main pass, then the heavy-chunk pass
 // (fm_match.cu).
@@ -208,6 +268,8 @@ struct ContextView {
     uint32_t def_cap;
     HeavyEntry* heavy;
     uint32_t heavy_cap;
+    SchedState* sched;     // persistent engine schedule (device)
+    SchedState* h_sched;   // pinned mirror
 };
 ContextView context_view(fm_context* c);
 

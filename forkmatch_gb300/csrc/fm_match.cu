@@ -36,6 +36,7 @@
 // `stop`, and exits; the host drains the output level (depth first) and
 // relaunches this level on the deferred chunks plus the unclaimed remainder.
 // Nothing spins and nothing traps.
+#include <algorithm>
 #include <mutex>
 #include <set>
 #include <utility>
@@ -103,12 +104,14 @@ __device__ __forceinline__ Tune make_tune(const ExpandParams& P, bool main_pass)
 }
 
 __device__ __forceinline__ uint32_t item_chunk(const ExpandParams& P, unsigned long long item) {
-    return item < P.ndef_in ? P.def_in[item] : (uint32_t)(P.fresh_base + (item - P.ndef_in));
+    return item < P.ndef_in ? P.def_in[(P.def_in_pos + item) % P.def_cap]
+                            : (uint32_t)(P.fresh_base + (item - P.ndef_in));
 }
 
 __device__ __forceinline__ void defer_chunk(const ExpandParams& P, uint32_t chunk) {
     const unsigned idx = atomicAdd(&P.ctl->ndef, 1u);
-    if (idx < P.def_cap) P.def_out[idx] = chunk;
+    const uint32_t room = P.def_room ? P.def_room : P.def_cap;
+    if (idx < room) P.def_out[(P.def_out_pos + idx) % P.def_cap] = chunk;
     else atomicOr(&P.ctl->error, 1u);
 }
 
@@ -353,11 +356,8 @@ __device__ __forceinline__ bool over_limit(const ExpandParams& P, uint32_t lane,
 // Main pass: warps claim batches of chunks; long candidate ranges are
 // published to the heavy list instead of being walked by one warp.
 template <int MODE, bool ROOTS, bool DUPS>
-__global__ void __launch_bounds__(kWarps * 32, 6) k_expand(const __grid_constant__ ExpandParams P) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ uint8_t col_depth_s[kMaxQ];
-    if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P.plan.col_depth[threadIdx.x];
-    __syncthreads();
+__device__ __forceinline__ void expand_main(const ExpandParams& P, unsigned char* smem_raw,
+                                            const uint8_t* col_depth_s) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t d = P.depth;
     const uint32_t k = P.plan.nreq[d];
@@ -469,16 +469,14 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_expand(const __grid_constant
     }
 }
 
-// Heavy pass (same stream, after the main pass): every warp claims pieces of
-// the published chunks, reloads that chunk and walks its piece of the slots.
-// The main pass already holds the chunk's output budget and counted its work.
+// Heavy pass (after the main pass): every warp claims pieces of the published
+// chunks, reloads that chunk and walks its piece of the slots -- the warps
+// that finished their own chunks take over the work of the hub chunks.  The
+// main pass already holds the chunk's output budget and counted its work.
 template <int MODE, bool ROOTS, bool DUPS>
-__global__ void __launch_bounds__(kWarps * 32, 6) k_expand_heavy(const __grid_constant__ ExpandParams P) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ uint8_t col_depth_s[kMaxQ];
-    if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P.plan.col_depth[threadIdx.x];
-    __syncthreads();
-    const unsigned long long h = P.ctl->heavy;
+__device__ __forceinline__ void expand_heavy(const ExpandParams& P, unsigned char* smem_raw,
+                                             const uint8_t* col_depth_s) {
+    const unsigned long long h = *(volatile unsigned long long*)&P.ctl->heavy;
     const uint32_t nent = (uint32_t)(h >> 32);
     const uint32_t npieces = (uint32_t)h;
     if (nent == 0) return;
@@ -517,6 +515,118 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_expand_heavy(const __grid_co
 }
 
 template <int MODE, bool ROOTS, bool DUPS>
+__global__ void __launch_bounds__(kWarps * 32, 6) k_expand(const __grid_constant__ ExpandParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint8_t col_depth_s[kMaxQ];
+    if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P.plan.col_depth[threadIdx.x];
+    __syncthreads();
+    expand_main<MODE, ROOTS, DUPS>(P, smem_raw, col_depth_s);
+}
+
+template <int MODE, bool ROOTS, bool DUPS>
+__global__ void __launch_bounds__(kWarps * 32, 6) k_expand_heavy(const __grid_constant__ ExpandParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint8_t col_depth_s[kMaxQ];
+    if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P.plan.col_depth[threadIdx.x];
+    __syncthreads();
+    expand_heavy<MODE, ROOTS, DUPS>(P, smem_raw, col_depth_s);
+}
+
+// ------------------------------------------------------- persistent engine
+//
+// One cooperative launch runs every level pass of the match.  A pass of depth
+// d is the same main and heavy pass as above, on the work items of the
+// depth-d queue: the deferred ring of depth d (chunks pushed back when the
+// output level filled) followed by the fresh chunks not yet claimed.  Between
+// passes block 0 advances the schedule (dev::sched_advance), so a level whose
+// output buffer fills is drained depth first on the device, with no host
+// round trip; a level whose chunks are long is cut into pieces that every warp
+// takes in the heavy pass.
+
+template <int LAST, bool DUPS>
+__device__ __forceinline__ void persist_main(const ExpandParams& P, unsigned char* smem, const uint8_t* cd,
+                                             bool roots, bool last) {
+    if (last) {
+        if (roots) expand_main<LAST, true, DUPS>(P, smem, cd);
+        else expand_main<LAST, false, DUPS>(P, smem, cd);
+    } else {
+        if (roots) expand_main<kModeMid, true, DUPS>(P, smem, cd);
+        else expand_main<kModeMid, false, DUPS>(P, smem, cd);
+    }
+}
+
+template <int LAST, bool DUPS>
+__device__ __forceinline__ void persist_heavy(const ExpandParams& P, unsigned char* smem, const uint8_t* cd,
+                                              bool roots, bool last) {
+    if (last) {
+        if (roots) expand_heavy<LAST, true, DUPS>(P, smem, cd);
+        else expand_heavy<LAST, false, DUPS>(P, smem, cd);
+    } else {
+        if (roots) expand_heavy<kModeMid, true, DUPS>(P, smem, cd);
+        else expand_heavy<kModeMid, false, DUPS>(P, smem, cd);
+    }
+}
+
+template <int LAST, bool DUPS>
+__global__ void __launch_bounds__(kWarps * 32, 5) k_persist(const __grid_constant__ ExpandParams P0,
+                                                            const __grid_constant__ PersistArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(16) ExpandParams P;          // level fields change per pass
+    __shared__ uint8_t col_depth_s[kMaxQ];
+    __shared__ unsigned flag_s, cur_s;
+    SchedState* S = A.sched;
+    {
+        const uint32_t* src = (const uint32_t*)&P0;
+        uint32_t* dst = (uint32_t*)&P;
+        for (uint32_t i = threadIdx.x; i < sizeof(ExpandParams) / 4; i += blockDim.x) dst[i] = src[i];
+    }
+    if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P0.plan.col_depth[threadIdx.x];
+    const uint32_t q = P0.plan.q;
+    bool first = true;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned d = *(volatile unsigned*)&S->cur;
+            if (*(volatile unsigned*)&S->error) d = 0;
+            cur_s = d;
+            if (d) {
+                const volatile SchedLevel* L = &S->lv[d];
+                const unsigned long long ring = L->tail - L->head;
+                const unsigned long long n_chunks = (L->n_parents + 31) / 32;
+                P.depth = d;
+                P.pin = d == 1 ? nullptr : A.levels[d];
+                P.pout = d + 1 < q ? A.levels[d + 1] : nullptr;
+                P.n_parents = L->n_parents;
+                P.ndef_in = (uint32_t)ring;
+                P.fresh_base = L->fresh;
+                P.n_items = ring + (n_chunks - L->fresh);
+                P.def_in = A.rings + (uint64_t)d * A.ring_cap;
+                P.def_out = A.rings + (uint64_t)d * A.ring_cap;
+                P.def_cap = A.ring_cap;
+                P.def_in_pos = L->head;
+                P.def_out_pos = L->tail;
+                P.def_room = A.ring_cap - (uint32_t)ring;
+                P.ctl = P0.ctl + d;
+            }
+        }
+        __syncthreads();
+        const unsigned d = cur_s;
+        if (d == 0) break;
+        const bool roots = d == 1, last = d + 1 == q;
+        persist_main<LAST, DUPS>(P, smem_raw, col_depth_s, roots, last);
+        if (!dev::grid_barrier(S, first && A.hold_first_barrier && blockIdx.x == 0, &flag_s)) break;
+        first = false;
+        persist_heavy<LAST, DUPS>(P, smem_raw, col_depth_s, roots, last);
+        if (!dev::grid_barrier(S, false, &flag_s)) break;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            const bool limit_hit = P.work_limit && (*(volatile unsigned*)&P.tot->error & kLimitFlag);
+            dev::sched_advance(S, P0.ctl, d, !last, P.n_items, P.ndef_in, P.def_room, limit_hit);
+        }
+        if (!dev::grid_barrier(S, false, &flag_s)) break;
+    }
+}
+
+template <int MODE, bool ROOTS, bool DUPS>
 void* kernel_ptr(bool heavy) {
     return heavy ? (void*)&k_expand_heavy<MODE, ROOTS, DUPS> : (void*)&k_expand<MODE, ROOTS, DUPS>;
 }
@@ -534,7 +644,72 @@ void* pick(int mode, bool roots, bool dups, bool heavy) {
     return nullptr;
 }
 
+void* persist_ptr(int last_mode, bool dups) {
+    if (last_mode == kModeLastTable) return dups ? (void*)&k_persist<kModeLastTable, true> : (void*)&k_persist<kModeLastTable, false>;
+    return dups ? (void*)&k_persist<kModeLastCount, true> : (void*)&k_persist<kModeLastCount, false>;
+}
+
 }  // namespace
+
+namespace {
+// Initial schedule: every pass starts at depth 1 on n_roots root rows.  A
+// kernel rather than a host copy, so a captured CUDA graph replays it.
+__global__ void k_sched_init(SchedState* S, unsigned q, unsigned long long n_roots, unsigned long long work_limit,
+                             unsigned long long wait_ns) {
+    unsigned* w = (unsigned*)S;
+    for (unsigned i = threadIdx.x; i < sizeof(SchedState) / 4; i += blockDim.x) w[i] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        S->cur = 1;
+        S->q = q;
+        S->work_limit = work_limit;
+        S->wait_limit_ns = wait_ns;
+        S->lv[1].n_parents = n_roots;
+    }
+}
+}  // namespace
+
+cudaError_t launch_sched_init(SchedState* S, unsigned q, unsigned long long n_roots, unsigned long long work_limit,
+                              unsigned long long wait_ns, cudaStream_t s) {
+    k_sched_init<<<1, 128, 0, s>>>(S, q, n_roots, work_limit, wait_ns);
+    return cudaGetLastError();
+}
+
+size_t persist_smem_bytes(const DevPlan& plan, const uint32_t* nreq_depth) {
+    size_t best = 0;
+    for (uint32_t d = 1; d < plan.q; d++) best = std::max<size_t>(best, per_warp_bytes(d, nreq_depth[d]));
+    return best * kWarps;
+}
+
+int persist_blocks_per_sm(int last_mode, bool dups, size_t smem) {
+    void* f = persist_ptr(last_mode, dups);
+    allow_dynamic_smem(f);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, kWarps * 32, smem) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    return n;
+}
+
+cudaError_t launch_persist(const ExpandParams& p, const PersistArgs& a, int last_mode, bool dups, int grid,
+                           size_t smem, cudaStream_t s) {
+    ExpandParams q = p;
+    q.max_warps = (uint32_t)grid * kWarps;
+    q.n_parents_dev = nullptr;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kWarps * 32);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void* args[] = {(void*)&q, (void*)&a};
+    return cudaLaunchKernelExC(&cfg, persist_ptr(last_mode, dups), args);
+}
 
 size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps) {
     return (size_t)warps * per_warp_bytes(depth, nreq);

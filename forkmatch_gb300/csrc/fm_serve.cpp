@@ -210,6 +210,9 @@ void fm_server::run_single(Slot& slot, Request* r, Lease& L, std::unique_lock<st
         o.host_rows = r->host_rows;
         o.host_rows_cap = r->host_cap;
         o.work_limit = opts.work_limit;
+        // slots overlap on the GPU: a cooperative launch needs the whole GPU
+        // resident at once, so served requests use level launches
+        o.engine = FM_ENGINE_LEVELS;
         st = fm_match(slot.ctx, graph, &r->query, &o, &res);
         r->res.attempts = attempt;
         r->res.lease_bytes = L.bytes;

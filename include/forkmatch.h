@@ -179,7 +179,28 @@ typedef struct fm_match_opts {
     uint64_t work_limit;        /* 0: none.  Otherwise stop once more than this many embeddings
                                    were counted, or partial matches produced, and return
                                    FM_ERR_LIMIT (count and rows are then a lower bound) */
+    int32_t engine;             /* fm_engine; profile = 1 always uses FM_ENGINE_LEVELS */
+    uint32_t wait_limit_ms;     /* persistent engine: bound on one grid-wide wait between level
+                                   passes (0: 60000).  A wait that runs out ends the match with
+                                   FM_ERR_DEVICE; the context stays usable */
+    int32_t test_stall_barrier; /* tests only: one block never arrives at the first grid
+                                   barrier, so every wait of it runs out (checks the bound) */
 } fm_match_opts;
+
+/* How the level passes of a match are driven.  Both replace the reference's
+ * dynamic-parallelism forks (src/smsm.cu:564-687, 949-1139) and give the same
+ * results.
+ *   FM_ENGINE_PERSISTENT: one cooperative launch per match.  Each depth has a
+ *     device work queue (a ring of chunks pushed back when the output level
+ *     filled, then the fresh chunks); the kernel schedules the passes depth
+ *     first on the device, and warps that finish their own chunks take pieces
+ *     of long (hub) chunks.  No host round trip between passes.
+ *   FM_ENGINE_LEVELS: one main + heavy launch pair per level pass; a level
+ *     whose output buffer filled is drained by the host, depth first. */
+typedef enum fm_engine {
+    FM_ENGINE_PERSISTENT = 0,
+    FM_ENGINE_LEVELS = 1
+} fm_engine;
 
 /* Matching order.  Results (count, row set, column layout) do not depend on
  * it; only the work does.  FM_ORDER_AUTO picks the order with the smallest
@@ -197,7 +218,7 @@ typedef struct fm_level_stats {
     uint64_t lookups;           /* (vertex, label) list lookups */
     uint64_t list_words;        /* sum of looked-up list lengths */
     uint64_t produced;          /* partial matches (or embeddings) produced */
-    uint32_t launches;
+    uint32_t launches;          /* passes of this depth */
     double kernel_ms;           /* sum of launch durations (profile = 1) */
 } fm_level_stats;
 
@@ -213,6 +234,9 @@ typedef struct fm_result {
     uint64_t h2d_bytes;         /* host->device bytes this match moved (kernel parameter blocks) */
     uint64_t d2h_bytes;         /* device->host bytes (control blocks, totals, copied rows) */
     fm_level_stats level[FM_MAX_QUERY_VERTICES];
+    int32_t engine;             /* fm_engine that ran */
+    uint32_t passes;            /* level passes over all depths */
+    uint64_t max_wait_ns;       /* persistent engine: longest grid-barrier wait of a block */
 } fm_result;
 
 fm_status fm_match(fm_context* ctx, const fm_graph* g, const fm_query* q,
@@ -220,9 +244,11 @@ fm_status fm_match(fm_context* ctx, const fm_graph* g, const fm_query* q,
 
 /* Batched matching.  No counterpart in the reference, which matches one query
  * per program run (src/smsm.cu:1182-1349): a batch matches many compiled
- * queries against one resident graph in shared level launches (max(q) - 1 of
- * them, captured once as a CUDA graph and replayed), each query's results
- * identical to fm_match's.  In table mode the first run counts every query
+ * queries against one resident graph in shared level passes, each query's
+ * results identical to fm_match's.  A run is one persistent cooperative
+ * launch fed by per-depth work queues (FM_ENGINE_PERSISTENT), captured once as
+ * a CUDA graph and replayed; where that launch does not fit, max(q) - 1 level
+ * launch pairs.  In table mode the first run counts every query
  * (a counting replay) and then gives each one a table region of exactly its
  * size in OUTPUT_PREALLOC, in batch order while it lasts (a query that does
  * not fit gets FM_ERR_OUTPUT_OVERFLOW; counts stay exact).  Queries with one
@@ -236,7 +262,10 @@ typedef struct fm_batch_stats {
     uint32_t batched_queries;   /* queries in the shared launches */
     uint32_t single_queries;    /* queries matched one by one */
     uint32_t piece_shift;       /* tuned: split-piece size = base << piece_shift */
-    uint32_t grid_quarters;     /* tuned: main-pass grid in quarters of a full grid */
+    uint32_t grid_quarters;     /* tuned: grid in quarters of the resident blocks per SM */
+    uint64_t level_rows;        /* tuned: rows per level buffer (the bank size) */
+    int32_t persistent;         /* 1: one cooperative launch per run (FM_ENGINE_PERSISTENT) */
+    int32_t graph;              /* 1: the run is a captured CUDA graph replay */
 } fm_batch_stats;
 
 fm_status fm_batch_create(fm_context* ctx, const fm_graph* g, const fm_query* const* queries, uint32_t n,
@@ -254,8 +283,12 @@ fm_status fm_batch_copy_rows(const fm_batch* b, uint32_t i, uint32_t* host, uint
  * too small (nothing copied). */
 fm_status fm_batch_copy_tables(const fm_batch* b, uint32_t* host, uint64_t cap_words, uint64_t* offsets,
                                uint64_t* words);
-/* Autotuner: runs the batch under each candidate split granularity and grid
- * size, keeps the fastest for later runs. */
+/* Engine of later runs (fm_engine; default FM_ENGINE_PERSISTENT).  Results
+ * do not depend on it. */
+fm_status fm_batch_set_engine(fm_batch* b, int32_t engine);
+/* Autotuner: runs the batch under each candidate split granularity (the
+ * intersection tile a warp walks), grid (warps in flight per SM) and level
+ * buffer size (the bank size), keeps the fastest for later runs. */
 fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best);
 void fm_batch_free(fm_batch* b);
 

@@ -73,3 +73,34 @@ def star_graph(d, label=1):
     c = np.zeros(d, dtype=np.uint32)
     leaves = np.arange(1, d + 1, dtype=np.uint32)
     return d + 1, np.concatenate([c, leaves]), np.concatenate([leaves, c]), np.full(2 * d, label, dtype=np.uint32)
+
+
+def table_sha(rows):
+    """SHA-256 of a table's rows sorted lexicographically (u32 little endian)."""
+    a = np.asarray(rows, dtype=np.uint32)
+    if a.size:
+        a = a[np.lexsort(a.T[::-1])]
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<u4").tobytes()).hexdigest()
+
+
+def reference_overflows_label_table(n_labels):
+    """Whether the reference's graph parser writes one label-graph entry past
+    its allocation for a data graph with n_labels edge labels: it allocates
+    n_labels + 1 entries of 88 bytes (rounded up to the next multiple of 128
+    bytes) and copies n_labels + 1 entries starting at entry 1
+    (src/trie.cuh:1115-1138, 1179).  The bytes past the allocation land on the
+    presence bitmaps of label 1's first vertices (src/trie.cuh:1162-1166)."""
+    size = 88 * (n_labels + 1)
+    return 88 > 128 - size % 128
+
+
+def reference_matches():
+    """(graph params, case, reference entry) for every query the reference's
+    own GPU build ran (tests/golden/ref_matches.json)."""
+    cases = {c["graph"]: {e["query"]: e for e in c["cases"]} for c in load_golden("match_cases.json")}
+    out = []
+    for g in load_golden("ref_matches.json")["graphs"]:
+        for e in g["cases"]:
+            if "count" in e:
+                out.append((g, cases[g["graph"]][e["query"]], e))
+    return out

@@ -1,0 +1,115 @@
+"""The persistent engine (one cooperative launch per match or batch, level
+passes scheduled on the device from per-depth work queues) against the level
+launch engine and the oracle: identical counts, tables and per-level work
+counters, with level buffers from ample down to a few chunks (so that the
+device drains levels depth first many times), and a grid-wide wait that runs
+out ends the match with FM_ERR_DEVICE while the context stays usable."""
+import numpy as np
+import pytest
+
+import forkmatch_gb300 as fm
+from forkmatch_gb300 import synth as S
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _sorted(a):
+    a = np.asarray(a, dtype=np.uint32)
+    return a[np.lexsort(a.T[::-1])] if a.size else a
+
+
+@pytest.fixture(scope="module")
+def graph():
+    from forkmatch_gb300 import build
+    build.build()
+    G = S.rmat(12, 30000, seed=21, n_elabels=2)
+    src, dst, lab = G.directed()
+    og = O.Graph.from_edges(G.V, 3, src, dst, lab)
+    rng = np.random.default_rng(5)
+    qs = [S.query_path(5, [1, 2, 1, 2]), S.query_cycle(4, [1, 2, 1, 2]), S.query_star(4, [1, 1, 2]),
+          S.query_clique(4, [1, 2]), S.query_path(2, [1])]
+    while len(qs) < 9:
+        q = S.query_random_walk(G, int(rng.integers(4, 7)), rng, bias=1.0)
+        if q is not None:
+            qs.append(q)
+    texts = [q.to_g_text() for q in qs]
+    want = [O.match(og, O.plan(t, enumerate_aut=0))[0] for t in texts]
+    return G, (src, dst, lab), og, texts, want
+
+
+@pytest.mark.parametrize("soln_mib", [1024, 64, 24])
+def test_engines_agree_from_ample_to_tiny_level_buffers(graph, soln_mib):
+    G, (src, dst, lab), og, texts, want = graph
+    ctx = fm.Context(prealloc_bytes=(soln_mib << 20) + (256 << 20), soln_prealloc_bytes=soln_mib << 20,
+                     output_prealloc_bytes=128 << 20, bank_rows=32)
+    g = fm.Graph.from_edges(ctx, G.V, 3, src, dst, lab)
+    deferred = 0
+    for t, w in zip(texts, want):
+        q = fm.Query.from_text(t)
+        a = fm.match(ctx, g, q, mode=fm.MODE_COUNT, engine=fm.ENGINE_PERSISTENT)
+        b = fm.match(ctx, g, q, mode=fm.MODE_COUNT, engine=fm.ENGINE_LEVELS)
+        assert a.count == b.count == w
+        assert a.engine == fm.ENGINE_PERSISTENT and a.launches == 1
+        for d in range(1, q.q):
+            la, lb = a.level[d], b.level[d]
+            assert (la.parents, la.lookups, la.list_words) == (lb.parents, lb.lookups, lb.list_words), d
+            if d + 1 < q.q:
+                assert la.produced == lb.produced, d
+        deferred += a.passes > q.q - 1
+        if w <= 1 << 20:
+            ca, ra, _ = fm.match_table(ctx, g, q, max_rows=max(1, w))
+            assert ca == w
+            buf = np.zeros(max(1, w) * q.q, dtype=np.uint32)
+            rb = fm.match(ctx, g, q, mode=fm.MODE_TABLE, host_rows=buf, engine=fm.ENGINE_LEVELS)
+            assert np.array_equal(_sorted(ra), _sorted(buf[: rb.rows_copied * q.q].reshape(-1, q.q)))
+    if soln_mib <= 64:
+        assert deferred >= 1          # the device drained at least one level depth first
+    g.close()
+    ctx.close()
+
+
+def test_persistent_wait_that_runs_out_returns_an_error_and_the_context_survives(graph):
+    """One block never arrives at the first grid barrier (a flag nothing
+    sets): every other block's wait runs out after wait_limit_ms, the kernel
+    returns, fm_match reports FM_ERR_DEVICE, and the next match on the same
+    context is exact."""
+    G, (src, dst, lab), og, texts, want = graph
+    ctx = fm.Context(prealloc_bytes=1 << 30, soln_prealloc_bytes=256 << 20, output_prealloc_bytes=128 << 20,
+                     bank_rows=32)
+    g = fm.Graph.from_edges(ctx, G.V, 3, src, dst, lab)
+    q = fm.Query.from_text(texts[0])
+    r = fm.match(ctx, g, q, mode=fm.MODE_COUNT, wait_limit_ms=200, test_stall_barrier=True,
+                 allow_device_error=True)
+    assert r.status == fm.FM_ERR_DEVICE and r.engine == fm.ENGINE_PERSISTENT
+    assert b"wait" in fm.lib().fm_last_error()
+    assert r.max_wait_ns >= 150_000_000
+    for t, w in zip(texts, want):
+        assert fm.match(ctx, g, fm.Query.from_text(t), mode=fm.MODE_COUNT).count == w
+    g.close()
+    ctx.close()
+
+
+def test_batch_engines_agree(graph):
+    G, (src, dst, lab), og, texts, want = graph
+    ctx = fm.Context(prealloc_bytes=1 << 30, soln_prealloc_bytes=48 << 20, output_prealloc_bytes=512 << 20,
+                     bank_rows=32)
+    g = fm.Graph.from_edges(ctx, G.V, 3, src, dst, lab)
+    queries = [fm.Query.from_text(t) for t in texts]
+    for mode in (fm.MODE_COUNT, fm.MODE_TABLE):
+        got = {}
+        for engine in (fm.ENGINE_PERSISTENT, fm.ENGINE_LEVELS):
+            b = fm.Batch(ctx, g, queries, mode=mode)
+            b.set_engine(engine)
+            for _ in range(2):                 # first run captures, the second replays
+                counts, st = b.run()
+                assert counts == want
+                assert st.persistent == (engine == fm.ENGINE_PERSISTENT)
+            if mode == fm.MODE_TABLE:
+                got[engine] = [_sorted(b.rows(i, max(1, want[i]))) for i in range(len(queries))]
+            b.close()
+        if mode == fm.MODE_TABLE:
+            for x, y in zip(got[fm.ENGINE_PERSISTENT], got[fm.ENGINE_LEVELS]):
+                assert np.array_equal(x, y)
+    g.close()
+    ctx.close()

@@ -12,7 +12,8 @@ import pytest
 import forkmatch_gb300 as fm
 from forkmatch_gb300 import synth as S
 from oracle import oracle as O
-from tests.helpers import complete_graph, cycle_graph, golden_graphs, star_graph
+from tests.helpers import (complete_graph, cycle_graph, golden_graphs, make_graph, reference_matches, star_graph,
+                           table_sha)
 
 pytestmark = pytest.mark.gpu
 
@@ -85,6 +86,31 @@ def test_golden_cases_count_table_and_work_counters(ctx):
             n += 1
             assert c == e["count"]
     assert n > 50
+
+
+def test_counts_and_tables_equal_the_reference_gpu_build(ctx):
+    """Every query the reference's own GPU matcher ran (tests/golden/
+    ref_matches.json): our count and sorted table equal its count and table,
+    under both engines, except for the cases the reference gets wrong (edge
+    label 1 on a graph whose label count makes it write past its label-graph
+    table), where they equal the oracle's."""
+    graphs = {}
+    n = 0
+    for g, case, ref in reference_matches():
+        key = g["graph"]
+        if key not in graphs:
+            graphs[key] = fm.Graph.from_text(ctx, make_graph(g["params"]).to_g_text())
+        q = fm.Query.from_text(case["text"].encode())
+        want_count = ref["count"] if ref["agrees_with_oracle"] else ref["oracle_count"]
+        want_sha = ref["table_sha256"] if ref["agrees_with_oracle"] else ref["oracle_table_sha256"]
+        for engine in (fm.ENGINE_PERSISTENT, fm.ENGINE_LEVELS):
+            assert fm.match(ctx, graphs[key], q, mode=fm.MODE_COUNT, engine=engine).count == want_count
+        cnt, rows, _ = fm.match_table(ctx, graphs[key], q, max_rows=max(1, want_count))
+        assert cnt == want_count and table_sha(rows) == want_sha
+        n += 1
+    assert n >= 60
+    for g in graphs.values():
+        g.close()
 
 
 @pytest.mark.parametrize("n", [5, 9, 33])
@@ -267,9 +293,10 @@ def test_level_overflow_deferral_gives_identical_results():
     q = S.query_path(5, [1, 2, 1, 2])
     p = O.plan(q.to_g_text(), enumerate_aut=0)
     oc = O.match(og, p)[0]
-    r = fm.match(small, g, fm.Query.from_text(q.to_g_text()), mode=fm.MODE_COUNT)
-    assert r.count == oc
-    assert r.launches > p.q - 1          # deferral happened
+    for engine in (fm.ENGINE_PERSISTENT, fm.ENGINE_LEVELS):
+        r = fm.match(small, g, fm.Query.from_text(q.to_g_text()), mode=fm.MODE_COUNT, engine=engine)
+        assert r.count == oc and r.engine == engine
+        assert r.passes > p.q - 1            # deferral happened
     small.close()
 
 

@@ -1,13 +1,14 @@
 """The CPU oracle: pinned against the reference planner's recorded outputs,
-closed-form counts and the committed golden match cases (no GPU needed)."""
+the reference GPU matcher's recorded counts and tables, closed-form counts and
+the committed golden match cases (no GPU needed)."""
 import math
 
 import pytest
 
 from forkmatch_gb300 import synth as S
 from oracle import oracle as O
-from tests.helpers import (complete_graph, cycle_graph, golden_graphs, load_golden, plan_to_ref_format,
-                           star_graph)
+from tests.helpers import (complete_graph, cycle_graph, golden_graphs, load_golden, make_graph, plan_to_ref_format,
+                           reference_matches, reference_overflows_label_table, star_graph, table_sha)
 
 
 @pytest.mark.parametrize("case", load_golden("ref_planner.json"), ids=lambda c: c["name"])
@@ -139,3 +140,42 @@ def test_star_closed_form_equals_oracle_count():
         q = S.query_star(len(leaves) + 1, leaves)
         c = O.match(og, O.plan(q.to_g_text(), enumerate_aut=0))[0]
         assert c == W.star_count_closed_form(G, leaves)
+
+
+_REF_GRAPHS = {}
+
+
+def _ref_graph(params):
+    key = tuple(sorted(params.items()))
+    if key not in _REF_GRAPHS:
+        _REF_GRAPHS[key] = O.Graph.parse(make_graph(params).to_g_text())
+    return _REF_GRAPHS[key]
+
+
+def test_reference_gpu_build_ran_on_enough_cases():
+    ran = reference_matches()
+    assert len(ran) >= 60
+    assert sum(1 for _, _, e in ran if e["agrees_with_oracle"]) >= 55
+    assert max(e["count"] for _, _, e in ran if e["agrees_with_oracle"]) > 300_000
+
+
+@pytest.mark.parametrize("g,case,ref", reference_matches(), ids=lambda x: x.get("query", x.get("graph", "")))
+def test_oracle_matches_reference_gpu_build(g, case, ref):
+    """The oracle's full count and sorted table equal what the reference's own
+    GPU matcher (built without SYMMETRY, run on a GB300) produced.  The only
+    cases where they differ are queries with edge label 1 on a graph whose
+    label count makes the reference write past its label-graph table (a
+    reference defect that corrupts label 1's presence bitmaps), and there the
+    oracle agrees with the library and with closed forms instead."""
+    og = _ref_graph(g["params"])
+    p = O.plan(case["text"].encode(), enumerate_aut=0)
+    c, rows, _ = O.match(og, p, table=True, table_cap=max(1, case["count"]))
+    assert c == case["count"] == ref["oracle_count"]
+    assert table_sha(rows) == ref["oracle_table_sha256"]
+    if ref["agrees_with_oracle"]:
+        assert ref["count"] == c and ref["table_sha256"] == table_sha(rows)
+        if "rows" in ref:
+            assert table_sha(ref["rows"]) == ref["table_sha256"]
+    else:
+        labels = {int(x.split()[3]) for x in case["text"].split("\n") if x.startswith("e ")}
+        assert reference_overflows_label_table(g["params"]["n_elabels"]) and 1 in labels

@@ -33,7 +33,7 @@ def setup():
     ctx.close()
 
 
-def _check_twice(ctx, g, q, torch, max_rows=1 << 20):
+def _check_twice(ctx, g, q, torch, max_rows=1 << 22):
     want_count, want_rows, _ = fm.match_table(ctx, g, q, max_rows=max_rows)
     assert want_count > 0 and want_rows.shape[0] == want_count
     buf = torch.zeros((want_count + 16) * q.q, dtype=torch.int32, device="cuda")
