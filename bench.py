@@ -78,28 +78,50 @@ def parse_args():
 
 def run_ncu_step(args):
     """One step of the workload with small knobs, for ncu captures (prints the
-    total count; every count is checked against the recorded one)."""
+    total count; every count is checked against the recorded one).  With
+    --workload ingest: the device parse and graph build of a 2^20-vertex,
+    8M-edge R-MAT graph as .g text (about 170 MB)."""
     import forkmatch_gb300 as fm
+    if args.workload == "ingest":
+        from forkmatch_gb300 import synth as S
+        G = S.rmat(20, 8_000_000, 13, 64)
+        text = G.to_g_text()
+        ctx = fm.Context(prealloc_bytes=1 * GB, soln_prealloc_bytes=256 << 20, output_prealloc_bytes=256 << 20)
+        g = fm.Graph.from_text(ctx, text)
+        inf = g.info()
+        print("ncu step ok", len(text), inf.edges, inf.segments)
+        g.close()
+        ctx.close()
+        return 0
     wl, G, (src, dst, lab), same, _ = load_workload(args.workload)
-    ctx = fm.Context(prealloc_bytes=7 * GB, soln_prealloc_bytes=2 * GB, output_prealloc_bytes=int(4.5 * GB),
-                     bank_rows=1 << 12)
-    g = fm.Graph.from_edges(ctx, G.V, G.n_elabels + 1, src, dst, lab)
     pick = None if args.queries == "all" else {int(x) for x in args.queries.split(",")}
+    # the table region only as large as the picked table queries need
+    need = sum(q["count"] * q["k"] * 4 for i, q in enumerate(wl["queries"])
+               if (pick is None or i in pick) and not is_count_only(q))
+    out_bytes = min(int(4.5 * GB), ((need + (64 << 20)) >> 20) << 20)
+    ctx = fm.Context(prealloc_bytes=2 * GB + out_bytes + (128 << 20), soln_prealloc_bytes=2 * GB,
+                     output_prealloc_bytes=out_bytes, bank_rows=1 << 12)
+    g = fm.Graph.from_edges(ctx, G.V, G.n_elabels + 1, src, dst, lab)
     if args.workload == "batched":
         # one batch (table mode, as in the benchmark) of the picked queries;
         # their algorithmic bytes come first from the plain kernels' counters
         # (k_expand launches, outside a k_bexpand capture filter)
         idx = [i for i in range(len(wl["queries"])) if pick is None or i in pick]
         qs = [fm.Query.from_text(wl["queries"][i]["text"].encode()) for i in idx]
+        counted = [is_count_only(wl["queries"][i]) for i in idx]
         alg = 0
-        for q in qs:
+        for q, c_only in zip(qs, counted):
             qi = q.info()
-            r = fm.match(ctx, g, q, mode=fm.MODE_TABLE, profile=True)
+            r = fm.match(ctx, g, q, mode=fm.MODE_COUNT if c_only else fm.MODE_TABLE, profile=True)
             for d in range(1, qi.q):
                 lv = r.level[d]
-                alg += 16 * lv.lookups + 4 * lv.list_words + 8 * lv.produced
-            alg += 4 * qi.q * r.count
+                rule = c_only and d == qi.q - 1 and qi.nreq[d] == 1
+                alg += 16 * lv.lookups + (0 if rule else 4 * lv.list_words) + 8 * lv.produced
+            alg += 0 if c_only else 4 * qi.q * r.count
         b = fm.Batch(ctx, g, qs, mode=fm.MODE_TABLE)
+        for i, c_only in enumerate(counted):
+            if c_only:
+                b.set_query_mode(i, fm.MODE_COUNT)
         counts, _ = b.run()
         if same and counts != [wl["queries"][i]["count"] for i in idx]:
             raise SystemExit("count mismatch in the batch")
@@ -244,6 +266,11 @@ def oracle_sample(wl, every):
     return [i for i in range(len(wl["queries"])) if i % every == 0]
 
 
+def is_count_only(qm):
+    """Queries recorded as count only (their tables have 10^9 rows or more)."""
+    return qm.get("mode", "table") == "count"
+
+
 def run_reference(args, rank, world):
     """The reference arm: the project's CPU port of the reference's algorithm
     (the reference has no CPU matcher of its own) on all host threads.  The
@@ -264,13 +291,13 @@ def run_reference(args, rank, world):
     warm = min(sample, key=lambda i: wl["queries"][i]["count"])
 
     for _ in range(args.warmup):
-        O.match(og, plans[warm], threads=threads)
+        O.match(og, plans[warm], threads=threads, count_rule=is_count_only(wl["queries"][warm]))
     t0 = time.perf_counter()
     total = 0
     counts = {}
     for part in parts:
         for i in part:
-            c = O.match(og, plans[i], threads=threads)[0]
+            c = O.match(og, plans[i], threads=threads, count_rule=is_count_only(wl["queries"][i]))[0]
             counts[i] = c
             total += c
     el = time.perf_counter() - t0
@@ -500,7 +527,7 @@ def run_ours(args, rank, world, local):
 
 def batched_config(wl, G, same):
     from collections import Counter
-    shapes = Counter(q["shape"] for q in wl["queries"])
+    shapes = Counter(q["shape"] + (" (count only)" if is_count_only(q) else "") for q in wl["queries"])
     sizes = Counter(q["k"] for q in wl["queries"])
     return {"workload": "batched", "graph": "R-MAT(0.57,0.19,0.19,0.05) 2^22 vertices, 64M undirected edges "
             "(128M e-lines), 64 edge labels, 8 vertex labels uniform", "vertices": G.V, "e_lines": wl["E"],
@@ -508,11 +535,13 @@ def batched_config(wl, G, same):
                                                                                       max(sizes.values())),
             "query_mix": dict(shapes),
             "excluded_shapes": sorted({"%s%d" % (x["shape"], x["k"]) for x in wl["excluded"]}),
-            "screening": "kept when the oracle finishes within 2^27 search nodes with count <= 2^22; paths, stars "
-                         "and cycles > 4 vertices exceed it on this graph and their slots hold walk subgraphs",
-            "mode": "batched: shared level launches for all queries replayed as one CUDA graph, autotuned "
-                    "split granularity and grid; per-query uint64 counts + uint32 tables. plain: one fm_match "
-                    "per query (table mode)",
+            "screening": "table queries: kept when the oracle finishes within 2^27 search nodes with count <= "
+                         "2^22; count-only queries: 4-vertex paths and stars pinned by exact closed forms, "
+                         "5-vertex paths by the oracle with the count rule; larger paths, stars and cycles are "
+                         "excluded with GPU time estimates (their slots hold walk subgraphs)",
+            "mode": "batched: one persistent cooperative launch for all queries replayed as a CUDA graph, "
+                    "autotuned split granularity, grid and level-buffer size; per-query uint64 counts + uint32 "
+                    "tables (count-only queries: counts). plain: one fm_match per query",
             "graph_matches_recorded_hash": same,
             "l2": "inputs larger than L2: resident graph 5.7 GB vs 129 MB L2; no flush between steps"}
 
@@ -562,7 +591,9 @@ def run_batched(args, rank, world, local):
         mine = list(range(len(meta_all)))
     meta = [meta_all[i] for i in mine]
     rec = [q["count"] for q in meta]
-    table_words = sum(q["count"] * q["k"] for q in meta)
+    counted = [is_count_only(q) for q in meta]
+    modes = [fm.MODE_COUNT if c else fm.MODE_TABLE for c in counted]
+    table_words = sum(q["count"] * q["k"] for q, c in zip(meta, counted) if not c)
     out_bytes = ((table_words * 4 + (256 << 20)) >> 20) << 20
     # one shared level buffer per depth holds every query's partial matches
     ctx = fm.Context(prealloc_bytes=128 * GB + out_bytes + (128 << 20), soln_prealloc_bytes=128 * GB,
@@ -576,8 +607,8 @@ def run_batched(args, rank, world, local):
 
     def plain_step(collect=None, profile=False):
         c = launches = 0
-        for q in queries:
-            r = fm.match(ctx, g, q, mode=fm.MODE_TABLE, profile=profile)
+        for q, mode in zip(queries, modes):
+            r = fm.match(ctx, g, q, mode=mode, profile=profile)
             c += r.count
             launches += r.launches
             if collect is not None:
@@ -589,24 +620,32 @@ def run_batched(args, rank, world, local):
     plain_step(collect=res)
     plain_counts = [r.count for r in res]
     rng = np.random.default_rng(7)
-    sample = sorted(rng.choice(len(meta), size=min(24, len(meta)), replace=False).tolist())
+    tabled = [i for i in range(len(meta)) if not counted[i]]
+    sample = sorted(rng.choice(tabled, size=min(24, len(tabled)), replace=False).tolist())
     plain_rows = {}
     for i in sample:
         cnt, rows, _ = fm.match_table(ctx, g, queries[i], max_rows=max(1, rec[i]))
         plain_rows[i] = rows[np.lexsort(rows.T[::-1])] if len(rows) else rows
 
     # roofline numerator: the algorithmic bytes of every query (same matching
-    # order in both forms), from the plain form's per-level counters
+    # order in both forms), from the plain form's per-level counters.  A
+    # count-only query's last level reads one record per parent and tests the
+    # parent's vertices against it (the count rule), so its list words are not
+    # charged; a table query's rows are.
     prof = []
     plain_step(collect=prof, profile=True)
     alg_bytes = 0
-    for r, qi in zip(prof, qinfo):
+    for r, qi, c_only in zip(prof, qinfo, counted):
         for d in range(1, qi.q):
             lv = r.level[d]
-            alg_bytes += 16 * lv.lookups + 4 * lv.list_words + 8 * lv.produced
-        alg_bytes += 4 * qi.q * r.count
+            rule = c_only and d == qi.q - 1 and qi.nreq[d] == 1
+            alg_bytes += 16 * lv.lookups + (0 if rule else 4 * lv.list_words) + 8 * lv.produced
+        alg_bytes += 0 if c_only else 4 * qi.q * r.count
 
     b = fm.Batch(ctx, g, queries, mode=fm.MODE_TABLE)
+    for i, c_only in enumerate(counted):
+        if c_only:
+            b.set_query_mode(i, fm.MODE_COUNT)
     b.run()
     tune = b.tune()
     counts, st = b.run()
@@ -658,6 +697,9 @@ def run_batched(args, rank, world, local):
     def e2e_fresh():
         qs = [fm.Query.from_text(tx) for tx in texts]
         bb = fm.Batch(ctx, g, qs, mode=fm.MODE_TABLE)
+        for i, c_only in enumerate(counted):
+            if c_only:
+                bb.set_query_mode(i, fm.MODE_COUNT)
         c, _ = bb.run()
         words, _ = bb.copy_tables(host)
         bb.close()
@@ -703,12 +745,16 @@ def run_batched(args, rank, world, local):
             "scaling": "strong", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generators)",
             "config": batched_config(wl, G, same),
             "embeddings_per_step": b_tot / args.steps,
+            "embeddings_per_step_by_mode": {
+                "table_queries": sum(c for c, co in zip(rec, counted) if not co),
+                "count_only_queries": sum(c for c, co in zip(rec, counted) if co)},
             "plain": {"value": plain_value, "ms_per_step": p_ms / args.steps, "launches_per_step":
                       p_launch / args.steps},
             "batched_over_plain": value / plain_value,
             "bitexact_counts": {"batched": batch_ok, "plain": plain_ok},
             "rows_equal_sample": {"queries": len(sample), "equal": rows_ok},
             "tuned": {"piece_shift": tune.piece_shift, "grid_quarters": tune.grid_quarters,
+                      "level_rows": tune.level_rows, "persistent": bool(st.persistent), "graph": bool(st.graph),
                       "batched_queries": st.batched_queries, "single_queries": st.single_queries},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": batched_traffic(alg_bytes / max(1, world)),
@@ -1017,8 +1063,8 @@ def cpu_baseline(wl, G, edges, name):
     plans = [O.plan(wl["queries"][i]["text"].encode(), enumerate_aut=0) for i in sample]
     t0 = time.perf_counter()
     c = 0
-    for p in plans:
-        c += O.match(og, p, threads=threads)[0]
+    for i, p in zip(sample, plans):
+        c += O.match(og, p, threads=threads, count_rule=is_count_only(wl["queries"][i]))[0]
     el = time.perf_counter() - t0
     model = cpu_model()
     return {"value": c / el, "unit": UNIT, "cores": threads, "kind": "port", "cpu_model": model,

@@ -41,7 +41,7 @@ EXPORTS = [
     "fm_match_static", "fm_batch_create", "fm_batch_run", "fm_batch_rows", "fm_batch_copy_rows", "fm_batch_tune",
     "fm_batch_free", "fm_batch_copy_tables", "fm_server_create", "fm_server_submit", "fm_server_poll",
     "fm_server_release", "fm_server_get_stats", "fm_server_destroy", "fm_graph_write_cache", "fm_table_write",
-    "fm_table_to_query_columns", "fm_batch_set_engine",
+    "fm_table_to_query_columns", "fm_batch_set_engine", "fm_batch_set_query_mode",
 ]
 
 
@@ -154,6 +154,7 @@ def lib():
         L.fm_batch_create.argtypes = [vp, vp, ctypes.POINTER(vp), u32, i32, ctypes.POINTER(vp)]
         L.fm_batch_run.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(BatchStats)]
         L.fm_batch_set_engine.argtypes = [vp, i32]
+        L.fm_batch_set_query_mode.argtypes = [vp, u32, i32]
         L.fm_batch_rows.argtypes = [vp, u32, ctypes.POINTER(vp), ctypes.POINTER(u64)]
         L.fm_batch_copy_rows.argtypes = [vp, u32, vp, u64, ctypes.POINTER(u64)]
         L.fm_batch_copy_tables.argtypes = [vp, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]
@@ -403,6 +404,9 @@ class Batch:
             ptr, cap = host.ctypes.data, host.size
         _check(lib().fm_batch_copy_tables(self._h, ptr, cap, offs, ctypes.byref(words)), "fm_batch_copy_tables")
         return words.value, [None if offs[i] == (1 << 64) - 1 else int(offs[i]) for i in range(n)]
+
+    def set_query_mode(self, i, mode):
+        _check(lib().fm_batch_set_query_mode(self._h, int(i), int(mode)), "fm_batch_set_query_mode")
 
     def set_engine(self, engine):
         _check(lib().fm_batch_set_engine(self._h, int(engine)), "fm_batch_set_engine")

@@ -33,6 +33,7 @@ struct BatchPlan {                    // per query, in device memory
     uint64_t table_cap;               // rows
     uint64_t root_off;                // roots: heads[root_off .. root_off + n_roots)
     uint32_t n_roots;
+    uint32_t count_only;              // no table for this query (count rule allowed)
 };
 
 struct BatchParams {
@@ -188,6 +189,17 @@ __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem
         }
         n = best;
         if (k > 2) drv = dev::order_lists(m.segs_s, lane, k, drv);
+        if (fin && k == 1 && (!P.table_mode || pl.count_only)) {
+            // Count rule (the query's count only): every entry of the single
+            // list extends the parent except the parent's own vertices, so the
+            // extensions are counted, not enumerated.
+            const uint4 sg = m.segs_s[lane];
+            unsigned long long c = sg.x;
+            for (uint32_t a = 0; a < d; a++)
+                c -= seg_has(sg, m.rows_s[a * 32 + lane], 1, P.nbr, P.bm, P.bm_words) ? 1u : 0u;
+            if (c) atomicAdd(&P.qpos[qid], c);
+            n = 0;
+        }
     }
     k_out = k;
     uint32_t incl = n;
@@ -588,6 +600,7 @@ struct fm_batch {
     cudaGraphExec_t exec[2] = {nullptr, nullptr};   // captured level sequence: count mode, table mode
     std::vector<BatchPlan> h_plans;                  // host copy (table regions are resized)
     bool regions_exact = false;                      // table regions sized from exact counts
+    bool plans_dirty = false;                        // h_plans changed since the last upload
     bool replay = true;                              // capture the level sequence as a CUDA graph
     bool own_scratch = true;                         // d_plans, d_qpos, h_qpos allocated here
 
@@ -1086,6 +1099,11 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
             set_error("too many (query, root chunk) pairs in one batch; split the batch");
             return FM_ERR_UNSUPPORTED;
         }
+        if (b->plans_dirty) {
+            FM_CUDA(cudaMemcpyAsync(b->d_plans, b->h_plans.data(), nq * sizeof(BatchPlan), cudaMemcpyHostToDevice,
+                                    cv.stream));
+            b->plans_dirty = false;
+        }
         if (b->table && !b->regions_exact) {
             // First table run: count every query, then give each query a table
             // region of exactly its size (in order, while OUTPUT_PREALLOC lasts).
@@ -1095,9 +1113,9 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
             uint64_t off = 0;
             for (uint32_t i = 0; i < nq; i++) {
                 BatchPlan& bp = b->h_plans[i];
-                const uint64_t need = b->h_qpos[i] * bp.q;
+                const uint64_t need = bp.count_only ? 0 : b->h_qpos[i] * bp.q;
                 bp.table_base = off;
-                bp.table_cap = off + need <= words ? b->h_qpos[i] : 0;
+                bp.table_cap = (!bp.count_only && off + need <= words) ? b->h_qpos[i] : 0;
                 off += bp.table_cap * bp.q;
                 b->table_base[i] = bp.table_base;
                 b->table_cap[i] = bp.table_cap;
@@ -1111,7 +1129,7 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
         for (uint32_t i = 0; i < nq; i++) {
             const uint32_t qi = b->batched[i];
             b->counts[qi] = b->h_qpos[i];
-            if (b->table && b->h_qpos[i] > b->table_cap[i]) truncated = 1;
+            if (b->table && !b->h_plans[i].count_only && b->h_qpos[i] > b->table_cap[i]) truncated = 1;
         }
     }
     for (uint32_t qi = 0; qi < b->n; qi++)
@@ -1223,6 +1241,21 @@ fm_status fm_batch_copy_tables(const fm_batch* b, uint32_t* host, uint64_t cap_w
     }
     *words = end;
     return FM_OK;
+}
+
+fm_status fm_batch_set_query_mode(fm_batch* b, uint32_t i, int32_t mode) {
+    if (!b || i >= b->n || (mode != FM_MODE_TABLE && mode != FM_MODE_COUNT)) return FM_ERR_ARG;
+    for (size_t k = 0; k < b->batched.size(); k++) {
+        if (b->batched[k] != i) continue;
+        const uint32_t co = mode == FM_MODE_COUNT ? 1u : 0u;
+        if (b->h_plans[k].count_only != co) {
+            b->h_plans[k].count_only = co;
+            b->plans_dirty = true;
+            b->regions_exact = false;
+            b->drop_graphs();
+        }
+    }
+    return FM_OK;   // queries matched on their own are counted only anyway
 }
 
 fm_status fm_batch_set_engine(fm_batch* b, int32_t engine) {

@@ -50,6 +50,82 @@ __device__ __forceinline__ bool seg_has(const uint4& s, uint32_t x, uint32_t nee
     return pos < s.x && __ldg(a + pos) == x;
 }
 
+// ------------------------------------------------- staged membership lists
+//
+// A list tested for membership by many candidates of a chunk is copied once
+// into the warp's shared-memory stage with a TMA bulk copy and searched there.
+// Its record then holds the stage offset in the `off16` field with kStagedMark
+// set (global offsets stay below 2^31 sixteen-byte units).
+constexpr uint32_t kStagedMark = 0x80000000u;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+// Makes generic-proxy accesses to shared memory (and an mbarrier init)
+// visible to the async proxy before later bulk copies.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// One TMA bulk copy global -> shared (16-byte aligned ends, size a multiple
+// of 16 bytes), completing on `bar`.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// lower_bound of x in a[0, n) in shared memory
+__device__ __forceinline__ uint32_t lower_bound_s(const uint32_t* a, uint32_t n, uint32_t x) {
+    uint32_t lo = 0;
+    while (n > 0) {
+        const uint32_t half = n >> 1;
+        if (a[lo + half] < x) {
+            lo += half + 1;
+            n -= half + 1;
+        } else {
+            n = half;
+        }
+    }
+    return lo;
+}
+
+// seg_has for records that may point into the warp's stage.
+__device__ __forceinline__ bool seg_has_st(const uint4& s, uint32_t x, uint32_t need, const uint32_t* __restrict__ nbr,
+                                           const uint32_t* __restrict__ bm, uint32_t bm_words, const uint32_t* stage) {
+    if (s.x > 3 && (s.y & kStagedMark)) {
+        if (x > s.w || x < s.z) return false;
+        const uint32_t* a = stage + (s.y & ~kStagedMark);
+        const uint32_t pos = lower_bound_s(a, s.x, x) + need - 1;
+        return pos < s.x && a[pos] == x;
+    }
+    return seg_has(s, x, need, nbr, bm, bm_words);
+}
+
 // Reorder one parent's records (column `lane` of recs): the driver first, the
 // other lists shortest first, so a candidate meets the most selective
 // membership test first and most rejections take one test.  Returns the

@@ -71,6 +71,16 @@ uint64_t env_u64(const char* name, uint64_t dflt) {
     return (end && *end == 0) ? (uint64_t)x : dflt;
 }
 
+}  // namespace
+
+uint32_t fm::stage_words_knob() {
+    // a multiple of 4 words (16-byte bulk copies), at most 4096 words (16 KiB per warp)
+    static const uint32_t w = (uint32_t)std::min<uint64_t>(env_u64("FM_STAGE_WORDS", 0), 4096) & ~3u;
+    return w;
+}
+
+namespace {
+
 // [0, 4 KiB) control blocks, [4 KiB, 8 KiB) match totals and the persistent
 // schedule, [8 KiB, 48 MiB) deferred-chunk lists (two per depth, which the
 // persistent engine uses as one ring per depth), [48 MiB, 64 MiB) heavy-chunk
@@ -516,7 +526,8 @@ struct MatchRun {
         for (uint32_t d = 1; d < q; d++) {
             const int mode = mode_of(d);
             const bool roots = d == 1;
-            const size_t smem = expand_smem_bytes(d, nreq_depth[d], block / 32);
+            const size_t smem = expand_smem_bytes(d, nreq_depth[d], block / 32,
+                                                  nreq_depth[d] >= 2 ? base.stage_words : 0);
             const int per_sm = expand_blocks_per_sm(mode, roots, dups, smem, block);
             const int full = ctx->sms * per_sm;
             ExpandParams p = base;
@@ -585,7 +596,7 @@ struct MatchRun {
     fm_status run_persistent(uint64_t n_roots, const fm_match_opts& opts) {
         const uint32_t q = plan->q;
         const int last_mode = table ? kModeLastTable : kModeLastCount;
-        const size_t smem = persist_smem_bytes(base.plan, nreq_depth);
+        const size_t smem = persist_smem_bytes(base.plan, nreq_depth, base.stage_words);
         const int per_sm = persist_blocks_per_sm(last_mode, dups, smem);
         if (per_sm < 1) return FM_ERR_UNSUPPORTED;
         const int grid = ctx->sms * per_sm;
@@ -649,7 +660,8 @@ struct MatchRun {
         const uint32_t q = plan->q;
         const int mode = mode_of(d);
         const uint64_t n_chunks = (n_parents + 31) / 32;
-        const size_t smem = expand_smem_bytes(d, nreq_depth[d], block / 32);
+        const size_t smem =
+            expand_smem_bytes(d, nreq_depth[d], block / 32, nreq_depth[d] >= 2 ? base.stage_words : 0);
         const int per_sm = expand_blocks_per_sm(mode, roots, dups, smem, block);
         (void)q;
         while (true) {
@@ -888,6 +900,7 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         b.heavy = ctx->heavy;
         b.heavy_cap = ctx->heavy_cap;
         b.work_limit = opts.work_limit;
+        b.stage_words = stage_words_knob();
         run.work_limit = opts.work_limit;
         fm_status st = FM_ERR_UNSUPPORTED;
         out->engine = FM_ENGINE_LEVELS;

@@ -187,6 +187,10 @@ struct ExpandParams {
     // last level: stop once the count (or reserved table rows) exceeds this,
     // setting bit kLimitFlag in tot->error; 0 = no limit
     unsigned long long work_limit;
+    // words of each warp's shared-memory stage for membership lists copied in
+    // by TMA (levels with two or more back edges); 0 = lists are searched in
+    // global memory
+    uint32_t stage_words;
 };
 constexpr unsigned int kLimitFlag = 2u;
 
@@ -234,7 +238,9 @@ struct PersistArgs {
 };
 
 // Dynamic shared memory and grid of the persistent kernel for a plan.
-size_t persist_smem_bytes(const DevPlan& plan, const uint32_t* nreq_depth);
+size_t persist_smem_bytes(const DevPlan& plan, const uint32_t* nreq_depth, uint32_t stage_words);
+// Words of the per-warp membership-list stage (FM_STAGE_WORDS, read once).
+uint32_t stage_words_knob();
 int persist_blocks_per_sm(int last_mode, bool dups, size_t smem);
 cudaError_t launch_persist(const ExpandParams& p, const PersistArgs& a, int last_mode, bool dups, int grid,
                            size_t smem, cudaStream_t s);
@@ -246,7 +252,7 @@ cudaError_t launch_sched_init(SchedState* S, unsigned q, unsigned long long n_ro
 // (fm_match.cu).
 cudaError_t launch_expand(const ExpandParams& p, int mode, bool roots, bool dups, int grid, int heavy_grid,
                           int block, size_t smem, cudaStream_t s);
-size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps);
+size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps, uint32_t stage_words);
 // Let kernel f launch with up to the device's opt-in shared memory (once per
 // device; safe from several host threads).
 void allow_dynamic_smem(const void* f);

@@ -121,13 +121,13 @@ __device__ __forceinline__ void defer_chunk(const ExpandParams& P, uint32_t chun
 template <bool DUPS>
 __device__ __forceinline__ bool slot_check(const ExpandParams& P, uint32_t x, uint32_t t, uint32_t j, uint32_t dj,
                                            const uint4& ds, const uint4* segs_s, const uint32_t* rows_s,
-                                           uint32_t k, uint32_t d) {
+                                           uint32_t k, uint32_t d, const uint32_t* stage) {
     bool ok = true;
     uint32_t need = 1;
     if (DUPS) need = seg_rank(ds, t, x, P.nbr) + 1;
     for (uint32_t i = 0; i < k && ok; i++) {
         if (i == dj) continue;
-        ok = seg_has(segs_s[i * 32 + j], x, need, P.nbr, P.bm, P.bm_words);
+        ok = dev::seg_has_st(segs_s[i * 32 + j], x, need, P.nbr, P.bm, P.bm_words, stage);
     }
     for (uint32_t c = 0; c < d && ok; c++) ok = rows_s[c * 32 + j] != x;
     return ok;
@@ -141,14 +141,17 @@ struct WarpMem {
     uint32_t* drv_s;    // [32] driver list of each parent
     uint32_t* stp;      // [kStage] staged survivors: parent index in the level
     uint32_t* stx;      // [kStage] staged survivors: new vertex
+    uint64_t* mbar;     // completion barrier of the list stage's bulk copies
+    uint32_t* stage;    // [stage_words] membership lists copied in by TMA (optional)
 };
 
-__host__ __device__ constexpr uint32_t per_warp_bytes(uint32_t d, uint32_t k) {
-    return 128 * d + 512 * k + 256 + 8 * kStage;
+__host__ __device__ constexpr uint32_t per_warp_bytes(uint32_t d, uint32_t k, uint32_t stage_words = 0) {
+    return 128 * d + 512 * k + 256 + 8 * kStage + (stage_words ? 16 + 4 * stage_words : 0);
 }
 
-__device__ __forceinline__ WarpMem warp_mem(unsigned char* smem_raw, uint32_t warp, uint32_t d, uint32_t k) {
-    unsigned char* ws = smem_raw + warp * per_warp_bytes(d, k);
+__device__ __forceinline__ WarpMem warp_mem(unsigned char* smem_raw, uint32_t warp, uint32_t d, uint32_t k,
+                                            uint32_t stage_words) {
+    unsigned char* ws = smem_raw + warp * per_warp_bytes(d, k, stage_words);
     WarpMem m;
     m.rows_s = (uint32_t*)ws;
     m.segs_s = (uint4*)(ws + 128 * d);
@@ -156,7 +159,71 @@ __device__ __forceinline__ WarpMem warp_mem(unsigned char* smem_raw, uint32_t wa
     m.drv_s = m.excl_s + 32;
     m.stp = (uint32_t*)(ws + 128 * d + 512 * k + 256);
     m.stx = m.stp + kStage;
+    m.mbar = (uint64_t*)(ws + 128 * d + 512 * k + 256 + 8 * kStage);
+    m.stage = (uint32_t*)(ws + 128 * d + 512 * k + 256 + 8 * kStage + 16);
     return m;
+}
+
+// Membership lists longer than this many words are not staged.
+constexpr uint32_t kStageMaxList = 2048;
+// Bound on the polls of one stage's completion barrier.
+constexpr uint32_t kStageSpinLimit = 1u << 22;
+
+// Stage the membership lists of the loaded chunk: every lane's non-driver
+// lists of 4..kStageMaxList entries without a bitmap, when its parent has at
+// least two candidates, are copied into the warp's stage with TMA bulk copies
+// (lanes in order while the stage has room) and their records in segs_s are
+// pointed at the stage.  Lane 0 arms the barrier with the byte count, every
+// lane issues its own copies, and the warp waits for the phase, boundedly.
+// Returns false (warp-uniform) if the wait ran out; the error bit 2 of the
+// level's control block is then raised.
+__device__ __forceinline__ bool stage_lists(const ExpandParams& P, const WarpMem& m, uint32_t lane, uint32_t k,
+                                            uint32_t drv, uint32_t n, bool valid, uint32_t& phase) {
+    uint32_t want = 0;
+    if (valid && k >= 2 && n >= 2) {
+        for (uint32_t i = 0; i < k; i++) {
+            if (i == drv) continue;
+            const uint4 r = m.segs_s[i * 32 + lane];
+            if (r.x > 3 && r.x <= kStageMaxList && !(r.z & kBitmapMark)) want += (r.x + 3) & ~3u;
+        }
+    }
+    uint32_t incl = want;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if ((int)lane >= o) incl += t;
+    }
+    const bool fits = want && incl <= P.stage_words;
+    uint32_t bytes = fits ? want * 4 : 0;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
+    if (!bytes) return true;
+    // earlier generic reads of the stage come before the copies overwrite it
+    dev::fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) dev::mbar_arrive_expect_tx(m.mbar, bytes);
+    __syncwarp();
+    if (fits) {
+        uint32_t off = incl - want;
+        for (uint32_t i = 0; i < k; i++) {
+            if (i == drv) continue;
+            uint4 r = m.segs_s[i * 32 + lane];
+            if (r.x > 3 && r.x <= kStageMaxList && !(r.z & kBitmapMark)) {
+                const uint32_t words = (r.x + 3) & ~3u;
+                dev::bulk_copy_g2s(m.stage + off, P.nbr + (uint64_t)r.y * 4, words * 4, m.mbar);
+                r.y = dev::kStagedMark | off;
+                m.segs_s[i * 32 + lane] = r;
+                off += words;
+            }
+        }
+    }
+    bool ok = false;
+    for (uint32_t spin = 0; spin < kStageSpinLimit && !ok; spin++) ok = dev::mbar_try_wait(m.mbar, phase);
+    phase ^= 1u;
+    ok = __all_sync(kFull, ok);
+    if (!ok && lane == 0) atomicOr(&P.ctl->error, 2u);
+    __syncwarp();
+    return ok;
 }
 
 // Column c of parent p of the level being expanded.
@@ -232,7 +299,8 @@ __device__ __forceinline__ void flush_stage(const ExpandParams& P, const WarpMem
 template <bool ROOTS>
 __device__ __forceinline__ uint32_t load_chunk(const ExpandParams& P, const WarpMem& m, uint32_t chunk, uint32_t lane,
                                                uint32_t d, uint32_t k, uint32_t rb, unsigned long long n_parents,
-                                               bool& valid, unsigned long long& words) {
+                                               bool& valid, unsigned long long& words, uint32_t& phase,
+                                               bool& stage_ok) {
     const uint64_t p = (uint64_t)chunk * 32 + lane;
     valid = p < n_parents;
     if (ROOTS) {
@@ -259,6 +327,8 @@ __device__ __forceinline__ uint32_t load_chunk(const ExpandParams& P, const Warp
         n = best;
         if (k > 2) drv = dev::order_lists(m.segs_s, lane, k, drv);
     }
+    stage_ok = true;
+    if (P.stage_words && k >= 2) stage_ok = stage_lists(P, m, lane, k, drv, n, valid, phase);
     uint32_t incl = n;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -298,7 +368,8 @@ __device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpM
         for (uint32_t u = 0; u < kSlots; u++) {
             if (ok[u]) {
                 const uint32_t dj = m.drv_s[j[u]];
-                ok[u] = slot_check<DUPS>(P, x[u], t[u], j[u], dj, m.segs_s[dj * 32 + j[u]], m.segs_s, m.rows_s, k, d);
+                ok[u] = slot_check<DUPS>(P, x[u], t[u], j[u], dj, m.segs_s[dj * 32 + j[u]], m.segs_s, m.rows_s, k, d,
+                                         m.stage);
             }
         }
         const unsigned lt = (1u << lane) - 1u;
@@ -362,8 +433,15 @@ __device__ __forceinline__ void expand_main(const ExpandParams& P, unsigned char
     const uint32_t d = P.depth;
     const uint32_t k = P.plan.nreq[d];
     const uint32_t rb = P.plan.req_begin[d];
-    const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k);
+    const uint32_t sw = k >= 2 ? P.stage_words : 0;   // only levels with membership tests stage lists
+    const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k, sw);
     const Tune T = make_tune(P, true);
+    uint32_t phase = 0;
+    if (sw) {
+        if (lane == 0) dev::mbar_init(m.mbar, 1);
+        dev::fence_proxy_async_smem();
+        __syncwarp();
+    }
 
     unsigned long long n_count = 0, n_lookups = 0, n_words = 0, n_parents = 0;
     unsigned long long n_flushed = 0;  // part of n_count already added to tot->count (lane 0)
@@ -396,10 +474,35 @@ __device__ __forceinline__ void expand_main(const ExpandParams& P, unsigned char
                     break;
                 }
             }
-            bool valid;
+            bool valid, stage_ok;
             unsigned long long w;
-            const uint32_t total = load_chunk<ROOTS>(P, m, chunk, lane, d, k, rb, T.n_parents, valid, w);
+            const uint32_t total = load_chunk<ROOTS>(P, m, chunk, lane, d, k, rb, T.n_parents, valid, w, phase,
+                                                     stage_ok);
             last_chunk = chunk;
+            if (!stage_ok) {
+                done = true;
+                break;
+            }
+            if (MODE == kModeLastCount && !DUPS && k == 1) {
+                // Count rule: with one requirement every list entry extends the
+                // parent except the parent's own vertices, so each lane counts
+                // its parent's extensions as the list length minus the row's
+                // vertices found in the list; no candidate is enumerated.
+                unsigned long long c = 0;
+                if (valid) {
+                    const uint4 sg = m.segs_s[lane];
+                    c = sg.x;
+                    for (uint32_t a = 0; a < d; a++)
+                        c -= seg_has(sg, m.rows_s[a * 32 + lane], 1, P.nbr, P.bm, P.bm_words) ? 1u : 0u;
+                    n_lookups += k;
+                    n_words += w;
+                    n_parents += 1;
+                }
+#pragma unroll
+                for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+                n_count += c;
+                continue;
+            }
             if (MODE == kModeMid && total) {
                 int ok = 1;
                 if (lane == 0) {
@@ -484,8 +587,15 @@ __device__ __forceinline__ void expand_heavy(const ExpandParams& P, unsigned cha
     const uint32_t d = P.depth;
     const uint32_t k = P.plan.nreq[d];
     const uint32_t rb = P.plan.req_begin[d];
-    const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k);
+    const uint32_t sw = k >= 2 ? P.stage_words : 0;
+    const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k, sw);
     const Tune T = make_tune(P, false);
+    uint32_t phase = 0;
+    if (sw) {
+        if (lane == 0) dev::mbar_init(m.mbar, 1);
+        dev::fence_proxy_async_smem();
+        __syncwarp();
+    }
     unsigned long long n_count = 0, n_flushed = 0;
     uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
     uint32_t nst = 0;
@@ -504,10 +614,11 @@ __device__ __forceinline__ void expand_heavy(const ExpandParams& P, unsigned cha
         const HeavyEntry e = P.heavy[lo];
         const uint32_t begin = ((uint32_t)gp - e.piece0) * T.heavy_piece;
         const uint32_t end = min(begin + T.heavy_piece, e.total);
-        bool valid;
+        bool valid, stage_ok;
         unsigned long long w;
-        load_chunk<ROOTS>(P, m, e.chunk, lane, d, k, rb, T.n_parents, valid, w);
+        load_chunk<ROOTS>(P, m, e.chunk, lane, d, k, rb, T.n_parents, valid, w, phase, stage_ok);
         last_chunk = e.chunk;
+        if (!stage_ok) break;
         process_slots<MODE, ROOTS, DUPS>(P, m, e.chunk, begin, end, lane, d, k, col_depth_s, nst, n_count);
     }
     if (MODE != kModeLastCount && nst) flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s, last_chunk);
@@ -675,9 +786,10 @@ cudaError_t launch_sched_init(SchedState* S, unsigned q, unsigned long long n_ro
     return cudaGetLastError();
 }
 
-size_t persist_smem_bytes(const DevPlan& plan, const uint32_t* nreq_depth) {
+size_t persist_smem_bytes(const DevPlan& plan, const uint32_t* nreq_depth, uint32_t stage_words) {
     size_t best = 0;
-    for (uint32_t d = 1; d < plan.q; d++) best = std::max<size_t>(best, per_warp_bytes(d, nreq_depth[d]));
+    for (uint32_t d = 1; d < plan.q; d++)
+        best = std::max<size_t>(best, per_warp_bytes(d, nreq_depth[d], nreq_depth[d] >= 2 ? stage_words : 0));
     return best * kWarps;
 }
 
@@ -711,8 +823,8 @@ cudaError_t launch_persist(const ExpandParams& p, const PersistArgs& a, int last
     return cudaLaunchKernelExC(&cfg, persist_ptr(last_mode, dups), args);
 }
 
-size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps) {
-    return (size_t)warps * per_warp_bytes(depth, nreq);
+size_t expand_smem_bytes(uint32_t depth, uint32_t nreq, int warps, uint32_t stage_words) {
+    return (size_t)warps * per_warp_bytes(depth, nreq, stage_words);
 }
 
 void allow_dynamic_smem(const void* f) {

@@ -91,7 +91,7 @@ struct StaticRun {
         uint32_t* def_b = def_a + kStaticDefCap;
         uint32_t ndef_in = 0;
         uint64_t fresh = 0;
-        const size_t smem = expand_smem_bytes(d, nreq[d], block / 32);
+        const size_t smem = expand_smem_bytes(d, nreq[d], block / 32, 0);
         const int per_sm = expand_blocks_per_sm(mode, roots, dups, smem, block);
         // A launch defers at most 8 chunks per warp (the largest claim batch),
         // so a grid of at most kStaticDefCap / (8 * warps per block) blocks

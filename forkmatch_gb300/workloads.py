@@ -104,6 +104,66 @@ def star_count_closed_form(G, leaf_labels):
     return float(total.sum())
 
 
+def _label_matrix(G, label):
+    """Adjacency matrix of one edge label (both directions), int64 CSR."""
+    import scipy.sparse as sp
+    src, dst, lab = G.directed()
+    m = lab == label
+    return sp.csr_matrix((np.ones(int(m.sum()), dtype=np.int64), (src[m].astype(np.int64), dst[m].astype(np.int64))),
+                         shape=(G.V, G.V))
+
+
+def star_count_exact(G, leaf_labels):
+    """Exact embedding count of a star whose leaves carry `leaf_labels` on a
+    simple graph with one label per edge: sum over centres of the product,
+    per label, of the falling factorial of the centre's degree in that label
+    (the labels partition a vertex's neighbours, and leaves with the same
+    label are an ordered choice of distinct neighbours).  Integer arithmetic;
+    raises if a term could overflow int64."""
+    src, dst, lab = G.directed()
+    total = np.ones(G.V, dtype=np.int64)
+    bound = np.ones(G.V, dtype=np.float64)
+    for l in sorted(set(leaf_labels)):
+        k = leaf_labels.count(l)
+        d = np.bincount(src[lab == l], minlength=G.V).astype(np.int64)
+        for i in range(k):
+            f = np.maximum(d - i, 0)
+            total *= f
+            bound *= f.astype(np.float64)
+    if bound.max() >= 2.0 ** 62 or bound.sum() >= 2.0 ** 63:
+        raise OverflowError("star count exceeds int64")
+    return int(total.sum())
+
+
+def path4_count_exact(G, labels):
+    """Exact embedding count of the path a-b-c-d with edge labels (l1, l2, l3)
+    on a simple graph with one label per edge (no self loops), by inclusion-
+    exclusion over the walks a-b-c-d: the walks number
+    W = sum over l2-edges (b, c) of d1(b) d3(c); a walk is not injective only
+    when a = c (possible only if l1 = l2: c is then an l1-neighbour of b),
+    b = d (only if l2 = l3) or a = d (a common l1-neighbour of b and
+    l3-neighbour of c: T = sum over l2-edges (b, c) of |N1(b) & N3(c)|); a = c
+    together with b = d needs l1 = l2 = l3, and no other two coincide at once
+    (they would force a self loop).  So the count is
+    W - [l1=l2] sum d3(c) - [l2=l3] sum d1(b) - T + [l1=l2=l3] |E_l2|."""
+    l1, l2, l3 = labels
+    A1, A2, A3 = _label_matrix(G, l1), _label_matrix(G, l2), _label_matrix(G, l3)
+    d1 = np.asarray(A1.sum(axis=1)).ravel().astype(np.int64)
+    d3 = np.asarray(A3.sum(axis=1)).ravel().astype(np.int64)
+    A2c = A2.tocoo()
+    b, c = A2c.row.astype(np.int64), A2c.col.astype(np.int64)
+    W = int(np.sum(d1[b] * d3[c]))
+    xa = int(np.sum(d3[c])) if l1 == l2 else 0
+    xb = int(np.sum(d1[b])) if l2 == l3 else 0
+    T = 0
+    step = 1 << 16
+    for r0 in range(0, G.V, step):
+        blk = (A1[r0:r0 + step] @ A3).multiply(A2[r0:r0 + step])
+        T += int(blk.sum())
+    xab = len(b) if l1 == l2 == l3 else 0
+    return W - xa - xb - T + xab
+
+
 def plain_small_graph():
     p = PLAIN_SMALL
     return S.erdos_renyi(p["n"], p["m"], p["seed"], p["n_elabels"])

@@ -283,6 +283,11 @@ fm_status fm_batch_copy_rows(const fm_batch* b, uint32_t i, uint32_t* host, uint
  * too small (nothing copied). */
 fm_status fm_batch_copy_tables(const fm_batch* b, uint32_t* host, uint64_t cap_words, uint64_t* offsets,
                                uint64_t* words);
+/* Query i of a table-mode batch as count only (FM_MODE_COUNT): no table
+ * region, its count exact; for queries whose tables cannot be kept.  In count
+ * mode a last depth with a single back edge is counted from the list (length
+ * minus the vertices already matched) instead of enumerated. */
+fm_status fm_batch_set_query_mode(fm_batch* b, uint32_t i, int32_t mode);
 /* Engine of later runs (fm_engine; default FM_ENGINE_PERSISTENT).  Results
  * do not depend on it. */
 fm_status fm_batch_set_engine(fm_batch* b, int32_t engine);

@@ -427,6 +427,7 @@ typedef struct {
     uint64_t scan_limit;         /* stop after this many driver-list candidates (0 = none) */
     uint64_t scanned;            /* atomic */
     int aborted;                 /* atomic */
+    int count_rule;              /* count the last depth from its list when it has one requirement */
     pthread_mutex_t mu;
     ora_stats total;
 } mctx;
@@ -491,6 +492,20 @@ static void dfs(wctx* w, int d) {
     }
     int sym = (w->m->ref_sym && P->sym_count > 1) ? P->last_sym[d] : 0;
     uint32_t bound = sym ? w->f[d - sym] : 0;
+    if (w->m->count_rule && d == q - 1 && k == 1 && !sym && !w->m->rows) {
+        /* Count rule: with one requirement, the last vertex can be any entry
+         * of the list (duplicates included) except the vertices already
+         * matched, so the extensions are the list length minus the copies of
+         * each matched vertex in it.  Same count as enumerating them. */
+        uint64_t c = ln[0];
+        for (int a = 0; a < d; a++) {
+            uint64_t lo = lower_b(lp[0], ln[0], w->f[a]);
+            while (lo < ln[0] && lp[0][lo] == w->f[a]) { c--; lo++; }
+        }
+        w->st.partials[d] += c;
+        w->st.count += c;
+        return;
+    }
     uint64_t j = 0;
     while (j < ln[drv]) {
         uint32_t x = lp[drv][j];
@@ -551,9 +566,18 @@ static void* worker(void* arg) {
 int ora_match(const ora_graph* g, const ora_plan* p, int ref_symmetry,
               uint32_t root_begin, uint32_t root_end, int threads,
               uint32_t* rows, uint64_t rows_cap, uint64_t limit, uint64_t scan_limit, ora_stats* st) {
+    return ora_match_ex(g, p, ref_symmetry, root_begin, root_end, threads, rows, rows_cap, limit, scan_limit, 0,
+                        st);
+}
+
+int ora_match_ex(const ora_graph* g, const ora_plan* p, int ref_symmetry,
+                 uint32_t root_begin, uint32_t root_end, int threads,
+                 uint32_t* rows, uint64_t rows_cap, uint64_t limit, uint64_t scan_limit, int count_rule,
+                 ora_stats* st) {
     mctx m;
     memset(&m, 0, sizeof(m));
     m.g = g; m.p = p; m.ref_sym = ref_symmetry;
+    m.count_rule = count_rule;
     if (root_end > g->V) root_end = g->V;
     m.root_begin = root_begin; m.root_end = root_end;
     m.next_root = root_begin;

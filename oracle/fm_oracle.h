@@ -127,6 +127,14 @@ typedef struct {
 int ora_match(const ora_graph* g, const ora_plan* p, int ref_symmetry,
               uint32_t root_begin, uint32_t root_end, int threads,
               uint32_t* rows, uint64_t rows_cap, uint64_t limit, uint64_t scan_limit, ora_stats* st);
+/* ora_match with count_rule = 1: without a table, a last depth with a single
+ * requirement is counted from its list (length minus the copies of the
+ * vertices already matched) instead of being enumerated; the count is the
+ * same (not part of the reference, which always enumerates). */
+int ora_match_ex(const ora_graph* g, const ora_plan* p, int ref_symmetry,
+                 uint32_t root_begin, uint32_t root_end, int threads,
+                 uint32_t* rows, uint64_t rows_cap, uint64_t limit, uint64_t scan_limit, int count_rule,
+                 ora_stats* st);
 
 #ifdef __cplusplus
 }

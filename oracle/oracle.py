@@ -69,6 +69,9 @@ def lib():
         L.ora_match.argtypes = [vp, ctypes.POINTER(Plan), ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
                                 ctypes.c_int, vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
                                 ctypes.POINTER(Stats)]
+        L.ora_match_ex.argtypes = [vp, ctypes.POINTER(Plan), ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
+                                   ctypes.c_int, vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                   ctypes.c_int, ctypes.POINTER(Stats)]
         _lib = L
     return _lib
 
@@ -139,11 +142,13 @@ def plan(text, enumerate_aut=None):
 
 
 def match(graph, p, ref_symmetry=False, roots=None, threads=None, table=False, table_cap=None, limit=0,
-          scan_limit=0):
+          scan_limit=0, count_rule=False):
     """Enumerate embeddings.  Returns (count, rows or None, Stats).
     With ``limit`` > 0, raises OracleError(1000) once the search visited more
     than ``limit`` nodes (partial matches and embeddings); ``scan_limit``
-    does the same for the driver-list candidates the nodes scanned."""
+    does the same for the driver-list candidates the nodes scanned.
+    ``count_rule`` (count only): a last depth with one requirement is counted
+    from its list instead of enumerated (same count)."""
     V = graph.V
     rb, re_ = (0, V) if roots is None else roots
     if threads is None:
@@ -154,9 +159,9 @@ def match(graph, p, ref_symmetry=False, roots=None, threads=None, table=False, t
         cap = table_cap if table_cap is not None else 1 << 22
         rows = np.zeros((cap, p.q), dtype=np.uint32)
     st = Stats()
-    rc = lib().ora_match(graph._h, ctypes.byref(p), int(bool(ref_symmetry)), rb, re_, int(threads),
-                         rows.ctypes.data if rows is not None else None, cap, int(limit), int(scan_limit),
-                         ctypes.byref(st))
+    rc = lib().ora_match_ex(graph._h, ctypes.byref(p), int(bool(ref_symmetry)), rb, re_, int(threads),
+                            rows.ctypes.data if rows is not None else None, cap, int(limit), int(scan_limit),
+                            int(bool(count_rule)), ctypes.byref(st))
     if rc:
         raise OracleError(rc, "ora_match")
     if rows is not None:

@@ -31,7 +31,14 @@ workload_batched.json
     on average, hubs of degree 1.6e5) every path and star and every cycle of
     more than 4 vertices falls in that case.
 
-Usage: python tests/golden/make_workloads.py [plain_at_scale|batched]
+restore_count_only (run after "batched")
+    Puts the 4-vertex path and star classes and the 5-vertex paths back into
+    the mix as count-only queries (their tables have 10^9 to 10^11 rows),
+    pinned by exact closed forms (4 vertices) or the oracle with its count
+    rule (5-vertex paths); the other slots are unchanged.  The classes still
+    excluded get an estimate of the GPU time they would need.
+
+Usage: python tests/golden/make_workloads.py [plain_at_scale|batched|restore_count_only]
 """
 import json
 import os
@@ -205,6 +212,97 @@ def batched():
     print("total embeddings", tot, "table bytes", rows, "%.1fs" % (time.time() - t0))
 
 
+# Classes restored as count-only queries (their tables cannot be kept: 10^9 to
+# 10^11 rows each), with the source of their exact counts.
+COUNT_ONLY = {("path", 4): "closed form (workloads.path4_count_exact)",
+              ("star", 4): "closed form (workloads.star_count_exact)",
+              ("path", 5): "oracle with the count rule (oracle.match(count_rule=True))"}
+GPU_RATE = 2.5e10     # partial matches per second the GPU level passes reach on this graph (measured)
+
+
+def annotate_excluded(wl):
+    """Why each remaining class is excluded, from its recorded evidence."""
+    for ex in wl["excluded"]:
+        why = []
+        est = ex.get("gpu_estimate", {}).get("seconds_per_query")
+        homs = [float(p["homomorphisms"]) for p in ex["probes"] if isinstance(p, dict) and "homomorphisms" in p]
+        if est is not None and est >= 1.0:
+            why.append("about %.3g s of GPU time per query (10 per step), beyond the step budget" % est)
+        if homs and max(homs) > 2.0 ** 64:
+            why.append("its homomorphism count (%.3g, an upper bound) exceeds u64" % max(homs))
+        if ex["shape"] == "cycle" and (est is None or est < 1.0):
+            why.append("no exact count to pin it: cycles have no closed form here and the oracle needs more "
+                       "than 2^27 search nodes (GPU estimate %.2g s per query)" % (est or 0))
+        ex["reason"] = "; ".join(why)
+
+
+def restore_count_only():
+    """Put the path and star classes that can be matched and pinned back into
+    the batched mix as count-only queries (their slots held walk queries):
+    4-vertex paths and stars with exact closed-form counts, 5-vertex paths
+    counted by the oracle with the count rule.  Every other query stays as
+    recorded.  The remaining excluded classes get a GPU estimate beside their
+    probes: the partial matches the level before the last must enumerate (the
+    homomorphism count of the class one vertex smaller, recorded by its
+    probes) over the measured rate."""
+    path = os.path.join(HERE, "workload_batched.json")
+    wl = json.load(open(path))
+    t0 = time.time()
+    G = W.batched_graph()
+    src, dst, lab = G.directed()
+    assert W.edge_hash(src, dst, lab) == wl["edge_sha256"]
+    G.adjacency()
+    og = O.Graph.from_edges(G.V, G.n_elabels + 1, src, dst, lab)
+    print("graph %.1fs" % (time.time() - t0), flush=True)
+    rng = np.random.default_rng(20261206)
+    for qm in wl["queries"]:
+        qm.setdefault("mode", "table")
+    for qm in wl["queries"]:
+        key = (qm["requested"], qm["k"])
+        if key not in COUNT_ONLY:
+            continue
+        while True:
+            q = _draw(G, qm["requested"], qm["k"], rng)
+            if q is not None:
+                break
+        t = time.time()
+        labels = [l for _, _, l in q.edges]
+        if key == ("path", 4):
+            c = W.path4_count_exact(G, labels)
+        elif key == ("star", 4):
+            c = W.star_count_exact(G, labels)
+        else:
+            c = O.match(og, O.plan(q.to_g_text(), enumerate_aut=0), count_rule=True)[0]
+        qm.update({"shape": qm["requested"], "text": q.to_g_text().decode(), "edges": len(q.edges),
+                   "density": round(q.density, 4), "count": int(c), "mode": "count",
+                   "count_source": COUNT_ONLY[key], "oracle_seconds": round(time.time() - t, 3)})
+        print(qm["slot"], key, "count", c, "%.1fs" % (time.time() - t), flush=True)
+    hom = {}
+    for ex in wl["excluded"]:
+        v = [float(p["homomorphisms"]) for p in ex["probes"] if isinstance(p, dict) and "homomorphisms" in p]
+        if v:
+            hom[(ex["shape"], ex["k"])] = max(v)
+    kept = []
+    for ex in wl["excluded"]:
+        if (ex["shape"], ex["k"]) in COUNT_ONLY:
+            continue
+        prefix = ("path" if ex["shape"] == "cycle" else ex["shape"], ex["k"] - 1)
+        if prefix in hom:
+            ex["gpu_estimate"] = {
+                "partial_matches_before_last_level": "%.3g" % hom[prefix],
+                "seconds_per_query": round(hom[prefix] / GPU_RATE, 2),
+                "basis": "homomorphisms of the %s%d probes over %.1e partial matches/s" % (prefix[0], prefix[1],
+                                                                                         GPU_RATE)}
+        kept.append(ex)
+    wl["excluded"] = kept
+    annotate_excluded(wl)
+    wl["count_only_classes"] = {"%s%d" % k: v for k, v in COUNT_ONLY.items()}
+    with open(path, "w") as f:
+        json.dump(wl, f, indent=1)
+    print("restored", sum(1 for q in wl["queries"] if q["mode"] == "count"), "count-only queries",
+          "%.1fs" % (time.time() - t0))
+
+
 if __name__ == "__main__":
     which = sys.argv[1] if len(sys.argv) > 1 else "plain_at_scale"
-    {"plain_at_scale": plain_at_scale, "batched": batched}[which]()
+    {"plain_at_scale": plain_at_scale, "batched": batched, "restore_count_only": restore_count_only}[which]()

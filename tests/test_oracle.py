@@ -3,6 +3,8 @@ the reference GPU matcher's recorded counts and tables, closed-form counts and
 the committed golden match cases (no GPU needed)."""
 import math
 
+import numpy as np
+
 import pytest
 
 from forkmatch_gb300 import synth as S
@@ -179,3 +181,38 @@ def test_oracle_matches_reference_gpu_build(g, case, ref):
     else:
         labels = {int(x.split()[3]) for x in case["text"].split("\n") if x.startswith("e ")}
         assert reference_overflows_label_table(g["params"]["n_elabels"]) and 1 in labels
+
+
+@pytest.mark.parametrize("seed,n_labels", [(1, 2), (2, 3), (3, 1)])
+def test_closed_forms_for_paths_and_stars_equal_the_oracle(seed, n_labels):
+    """The exact closed forms that pin the 4-vertex path and star classes of
+    the batched workload (forkmatch_gb300.workloads) equal the oracle's
+    enumeration for every label combination, equal labels included."""
+    import itertools
+
+    from forkmatch_gb300 import workloads as W
+    G = S.rmat(11, 15000, seed, n_labels)
+    src, dst, lab = G.directed()
+    og = O.Graph.from_edges(G.V, n_labels + 1, src, dst, lab)
+    for labs in itertools.product(range(1, n_labels + 1), repeat=3):
+        for q, cf in ((S.query_path(4, list(labs)), W.path4_count_exact),
+                      (S.query_star(4, list(labs)), W.star_count_exact)):
+            p = O.plan(q.to_g_text(), enumerate_aut=0)
+            assert O.match(og, p)[0] == cf(G, list(labs))
+
+
+def test_count_rule_equals_enumeration():
+    """The count rule (a last depth with one back edge counted from its list)
+    gives the enumerated count, duplicates included."""
+    G = S.rmat(11, 15000, 4, 2)
+    src, dst, lab = G.directed()
+    for dup in (False, True):
+        if dup:   # repeat some e-lines (both directions) to make duplicates
+            k = len(src) // 7
+            src, dst, lab = (np.concatenate([src, src[:k]]), np.concatenate([dst, dst[:k]]),
+                             np.concatenate([lab, lab[:k]]))
+        og = O.Graph.from_edges(G.V, 3, src, dst, lab)
+        for q in (S.query_path(4, [1, 2, 1]), S.query_star(4, [1, 1, 2]), S.query_path(5, [1, 2, 2, 1]),
+                  S.query_cycle(4, [1, 2, 1, 2]), S.query_path(2, [2])):
+            p = O.plan(q.to_g_text(), enumerate_aut=0)
+            assert O.match(og, p)[0] == O.match(og, p, count_rule=True)[0]
