@@ -75,6 +75,7 @@ struct BatchParams {
     uint32_t heavy_cap;
     uint32_t max_warps;
     uint32_t piece_shift;                     // autotuned: heavy threshold and piece size scale
+    uint32_t stage_words;                     // per-warp membership-list stage (0: lists stay in global memory)
 };
 
 namespace {
@@ -125,14 +126,17 @@ struct BMem {
     uint32_t* stp;      // [kBStage] staged parent index
     uint32_t* stx;      // [kBStage] staged vertex
     uint32_t* stq;      // [kBStage] staged query id
+    uint64_t* mbar;     // completion barrier of the list stage's bulk copies
+    uint32_t* stage;    // [stage_words] membership lists copied in by TMA (optional)
 };
 
-__host__ __device__ constexpr uint32_t bper_warp_bytes(uint32_t d, uint32_t kmax) {
-    return 128 * d + 512 * kmax + 6 * 128 + 12 * kBStage;
+__host__ __device__ constexpr uint32_t bper_warp_bytes(uint32_t d, uint32_t kmax, uint32_t stage_words = 0) {
+    return 128 * d + 512 * kmax + 6 * 128 + 12 * kBStage + (stage_words ? 16 + 4 * stage_words : 0);
 }
 
-__device__ __forceinline__ BMem bmem(unsigned char* smem, uint32_t warp, uint32_t d, uint32_t kmax) {
-    unsigned char* w = smem + warp * bper_warp_bytes(d, kmax);
+__device__ __forceinline__ BMem bmem(unsigned char* smem, uint32_t warp, uint32_t d, uint32_t kmax,
+                                     uint32_t stage_words) {
+    unsigned char* w = smem + warp * bper_warp_bytes(d, kmax, stage_words);
     BMem m;
     m.rows_s = (uint32_t*)w;
     m.segs_s = (uint4*)(w + 128 * d);
@@ -146,13 +150,73 @@ __device__ __forceinline__ BMem bmem(unsigned char* smem, uint32_t warp, uint32_
     m.stp = s + 192;
     m.stx = m.stp + kBStage;
     m.stq = m.stx + kBStage;
+    m.mbar = (uint64_t*)(w + 128 * d + 512 * kmax + 6 * 128 + 12 * kBStage);
+    m.stage = (uint32_t*)(w + 128 * d + 512 * kmax + 6 * 128 + 12 * kBStage + 16);
     return m;
+}
+
+constexpr uint32_t kBStageMaxList = 2048;
+constexpr uint32_t kBStageSpinLimit = 1u << 22;
+
+// Stage the membership lists of a loaded chunk into the warp's stage with
+// TMA bulk copies (the same rule as the single-query kernel, with each lane's
+// own number of back edges k and driver drv): non-driver lists of
+// 4..kBStageMaxList entries without a bitmap, for parents with at least two
+// candidates, lanes in order while the stage has room.  Returns false
+// (warp-uniform) if the bounded wait ran out; error bit 2 is then raised.
+__device__ __forceinline__ bool bstage_lists(const BatchParams& P, const BMem& m, uint32_t lane, uint32_t k,
+                                             uint32_t drv, uint32_t n, bool valid, uint32_t sw, uint32_t& phase) {
+    uint32_t want = 0;
+    if (valid && k >= 2 && n >= 2) {
+        for (uint32_t i = 0; i < k; i++) {
+            if (i == drv) continue;
+            const uint4 r = m.segs_s[i * 32 + lane];
+            if (r.x > 3 && r.x <= kBStageMaxList && !(r.z & kBitmapMark)) want += (r.x + 3) & ~3u;
+        }
+    }
+    uint32_t incl = want;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if ((int)lane >= o) incl += t;
+    }
+    const bool fits = want && incl <= sw;
+    uint32_t bytes = fits ? want * 4 : 0;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) bytes += __shfl_xor_sync(kFull, bytes, o);
+    if (!bytes) return true;
+    dev::fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) dev::mbar_arrive_expect_tx(m.mbar, bytes);
+    __syncwarp();
+    if (fits) {
+        uint32_t off = incl - want;
+        for (uint32_t i = 0; i < k; i++) {
+            if (i == drv) continue;
+            uint4 r = m.segs_s[i * 32 + lane];
+            if (r.x > 3 && r.x <= kBStageMaxList && !(r.z & kBitmapMark)) {
+                const uint32_t words = (r.x + 3) & ~3u;
+                dev::bulk_copy_g2s(m.stage + off, P.nbr + (uint64_t)r.y * 4, words * 4, m.mbar);
+                r.y = dev::kStagedMark | off;
+                m.segs_s[i * 32 + lane] = r;
+                off += words;
+            }
+        }
+    }
+    bool ok = false;
+    for (uint32_t spin = 0; spin < kBStageSpinLimit && !ok; spin++) ok = dev::mbar_try_wait(m.mbar, phase);
+    phase ^= 1u;
+    ok = __all_sync(kFull, ok);
+    if (!ok && lane == 0) atomicOr(&P.ctl->error, 2u);
+    __syncwarp();
+    return ok;
 }
 
 template <bool ROOTS>
 __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem& m, uint32_t chunk, uint32_t lane,
                                                 uint32_t d, unsigned long long n_parents, bool& valid,
-                                                uint32_t& k_out, unsigned long long& words) {
+                                                uint32_t& k_out, unsigned long long& words, uint32_t sw,
+                                                uint32_t& phase, bool& stage_ok) {
     uint32_t qid, pidx;
     if (ROOTS) {
         qid = chunk / P.chunks_per_query;
@@ -201,6 +265,8 @@ __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem
             n = 0;
         }
     }
+    stage_ok = true;
+    if (sw) stage_ok = bstage_lists(P, m, lane, k, drv, n, valid, sw, phase);
     k_out = k;
     uint32_t incl = n;
 #pragma unroll
@@ -281,7 +347,7 @@ __device__ __forceinline__ void bprocess(const BatchParams& P, const BMem& m, ui
             const uint32_t k = m.k_s[j];
             for (uint32_t i = 0; i < k && ok; i++) {
                 if (i == dj) continue;
-                ok = seg_has(m.segs_s[i * 32 + j], x, 1, P.nbr, P.bm, P.bm_words);
+                ok = dev::seg_has_st(m.segs_s[i * 32 + j], x, 1, P.nbr, P.bm, P.bm_words, m.stage);
             }
             for (uint32_t c = 0; c < d && ok; c++) ok = m.rows_s[c * 32 + j] != x;
         }
@@ -321,8 +387,15 @@ template <bool ROOTS>
 __device__ __forceinline__ void bexpand_main(const BatchParams& P, unsigned char* smem_raw) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t d = P.depth;
-    const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax);
+    const uint32_t sw = P.kmax >= 2 ? P.stage_words : 0;   // only levels with membership tests stage lists
+    const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax, sw);
     const BTune T = make_btune(P);
+    uint32_t phase = 0;
+    if (sw) {
+        if (lane == 0) dev::mbar_init(m.mbar, 1);
+        dev::fence_proxy_async_smem();
+        __syncwarp();
+    }
     unsigned long long n_lookups = 0, n_words = 0, n_parents = 0, credit = 0;
     uint32_t nst = 0;
     uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
@@ -339,11 +412,13 @@ __device__ __forceinline__ void bexpand_main(const BatchParams& P, unsigned char
             if (lane == 0) bdefer(P, chunk);
             break;
         }
-        bool valid;
+        bool valid, stage_ok;
         uint32_t k;
         unsigned long long w;
-        const uint32_t total = bload_chunk<ROOTS>(P, m, chunk, lane, d, T.n_parents, valid, k, w);
+        const uint32_t total = bload_chunk<ROOTS>(P, m, chunk, lane, d, T.n_parents, valid, k, w, sw, phase,
+                                                  stage_ok);
         last_chunk = chunk;
+        if (!stage_ok) break;
         // only survivors of queries that go on use the next level's buffer;
         // the upper bound of the whole chunk is reserved (over-reserving is safe)
         if (total && P.pout) {
@@ -413,8 +488,15 @@ __device__ __forceinline__ void bexpand_heavy(const BatchParams& P, unsigned cha
     if (nent == 0) return;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t d = P.depth;
-    const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax);
+    const uint32_t sw = P.kmax >= 2 ? P.stage_words : 0;
+    const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax, sw);
     const BTune T = make_btune(P);
+    uint32_t phase = 0;
+    if (sw) {
+        if (lane == 0) dev::mbar_init(m.mbar, 1);
+        dev::fence_proxy_async_smem();
+        __syncwarp();
+    }
     uint32_t nst = 0;
     uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
     for (;;) {
@@ -431,11 +513,12 @@ __device__ __forceinline__ void bexpand_heavy(const BatchParams& P, unsigned cha
         const HeavyEntry e = P.heavy[lo];
         const uint32_t begin = ((uint32_t)gp - e.piece0) * T.heavy_piece;
         const uint32_t end = min(begin + T.heavy_piece, e.total);
-        bool valid;
+        bool valid, stage_ok;
         uint32_t k;
         unsigned long long w;
-        bload_chunk<ROOTS>(P, m, e.chunk, lane, d, T.n_parents, valid, k, w);
+        bload_chunk<ROOTS>(P, m, e.chunk, lane, d, T.n_parents, valid, k, w, sw, phase, stage_ok);
         last_chunk = e.chunk;
+        if (!stage_ok) break;
         bprocess<ROOTS>(P, m, e.chunk, begin, end, lane, d, nst);
     }
     if (nst) bflush<ROOTS>(P, m, nst, lane, d, last_chunk);
@@ -693,7 +776,9 @@ struct BatchRun {
         return cv.defs + (size_t)(2 * d + which) * cv.def_cap;
     }
     int gfull[kMaxQ] = {};
-    size_t smem(uint32_t d) const { return (size_t)kBWarps * bper_warp_bytes(d, b->kmax[d]); }
+    size_t smem(uint32_t d) const {
+        return (size_t)kBWarps * bper_warp_bytes(d, b->kmax[d], b->kmax[d] >= 2 ? base.stage_words : 0);
+    }
     // occupancy queries and attribute changes happen here, before any capture
     void prepare() {
         for (uint32_t d = 1; d < b->maxq; d++) gfull[d] = cv.sms * batch_blocks_per_sm(d == 1, smem(d));
@@ -706,7 +791,8 @@ struct BatchRun {
     int pgrid = 0;                        // persistent grid (0: level launches)
     size_t psmem() const {
         size_t m = 0;
-        for (uint32_t d = 1; d < b->maxq; d++) m = std::max<size_t>(m, bper_warp_bytes(d, b->kmax[d]));
+        for (uint32_t d = 1; d < b->maxq; d++)
+            m = std::max<size_t>(m, bper_warp_bytes(d, b->kmax[d], b->kmax[d] >= 2 ? base.stage_words : 0));
         return m * kBWarps;
     }
 
@@ -1095,6 +1181,7 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
         run.base.heavy = cv.heavy;
         run.base.heavy_cap = cv.heavy_cap;
         run.base.piece_shift = b->piece_shift;
+        run.base.stage_words = stage_words_knob();
         if ((uint64_t)nq * run.base.chunks_per_query >= (1ull << 32)) {
             set_error("too many (query, root chunk) pairs in one batch; split the batch");
             return FM_ERR_UNSUPPORTED;

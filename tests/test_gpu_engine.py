@@ -113,3 +113,54 @@ def test_batch_engines_agree(graph):
                 assert np.array_equal(x, y)
     g.close()
     ctx.close()
+
+
+_STAGED_CHECK = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+import forkmatch_gb300 as fm
+from forkmatch_gb300 import synth as S
+from oracle import oracle as O
+G = S.rmat(12, 40000, seed=23, n_elabels=2)
+src, dst, lab = G.directed()
+og = O.Graph.from_edges(G.V, 3, src, dst, lab)
+ctx = fm.Context(prealloc_bytes=1 << 30, soln_prealloc_bytes=64 << 20, output_prealloc_bytes=256 << 20, bank_rows=32)
+g = fm.Graph.from_edges(ctx, G.V, 3, src, dst, lab)
+qs = [S.query_cycle(4, [1, 2, 1, 2]), S.query_clique(4, [1, 2]), S.query_cycle(5, [1, 1, 2, 2, 1]),
+      S.query_clique(5, [2, 1])]
+want = [O.match(og, O.plan(q.to_g_text(), enumerate_aut=0))[0] for q in qs]
+queries = [fm.Query.from_text(q.to_g_text()) for q in qs]
+for engine in (fm.ENGINE_PERSISTENT, fm.ENGINE_LEVELS):
+    got = [fm.match(ctx, g, q, mode=fm.MODE_COUNT, engine=engine).count for q in queries]
+    assert got == want, (engine, got, want)
+for qq, q, w in zip(qs, queries, want):
+    if w <= 1 << 20:
+        c, rows, _ = fm.match_table(ctx, g, q, max_rows=max(1, w))
+        o = O.match(og, O.plan(qq.to_g_text(), enumerate_aut=0), table=True, table_cap=max(1, w))[1]
+        a = rows[np.lexsort(rows.T[::-1])]
+        b = o[np.lexsort(o.T[::-1])]
+        assert c == w and np.array_equal(a, b)
+b = fm.Batch(ctx, g, queries, mode=fm.MODE_COUNT)
+for _ in range(2):
+    counts, _ = b.run()
+    assert counts == want, (counts, want)
+print("staged ok", want)
+"""
+
+
+@pytest.mark.parametrize("words", [64, 1024])
+def test_staged_membership_lists_give_identical_results(words):
+    """With the per-warp stage on (FM_STAGE_WORDS, read once per process, so
+    the check runs in a child process), membership lists copied into shared
+    memory by TMA bulk copies give the oracle's counts and tables in both
+    engines and in a batch; 64 words forces most lists to stay in global
+    memory beside the staged ones."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, FM_STAGE_WORDS=str(words))
+    r = subprocess.run([sys.executable, "-c", _STAGED_CHECK, root], env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "staged ok" in r.stdout
