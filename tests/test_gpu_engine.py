@@ -27,14 +27,28 @@ def graph():
     src, dst, lab = G.directed()
     og = O.Graph.from_edges(G.V, 3, src, dst, lab)
     rng = np.random.default_rng(5)
-    qs = [S.query_path(5, [1, 2, 1, 2]), S.query_cycle(4, [1, 2, 1, 2]), S.query_star(4, [1, 1, 2]),
-          S.query_clique(4, [1, 2]), S.query_path(2, [1])]
-    while len(qs) < 9:
-        q = S.query_random_walk(G, int(rng.integers(4, 7)), rng, bias=1.0)
+    cands = [S.query_path(4, [1, 2, 1]), S.query_cycle(4, [1, 2, 1, 2]), S.query_star(4, [1, 1, 2]),
+             S.query_clique(4, [1, 2]), S.query_path(2, [1])]
+    for _ in range(40):
+        q = S.query_random_walk(G, int(rng.integers(4, 7)), rng, min_density=0.5, bias=1.0)
         if q is not None:
-            qs.append(q)
-    texts = [q.to_g_text() for q in qs]
-    want = [O.match(og, O.plan(t, enumerate_aut=0))[0] for t in texts]
+            cands.append(q)
+    # the oracle's counts (count rule: exact, pinned against enumeration on
+    # the CPU); queries it cannot finish within its node limit are dropped
+    texts, want = [], []
+    for q in cands:
+        t = q.to_g_text()
+        try:
+            c = O.match(og, O.plan(t, enumerate_aut=0), count_rule=True, limit=1 << 25)[0]
+        except O.OracleError:
+            continue
+        if c > 500_000_000:          # keeps the level-launch engine's host drains short
+            continue
+        texts.append(t)
+        want.append(c)
+        if len(texts) == 9:
+            break
+    assert len(texts) >= 7
     return G, (src, dst, lab), og, texts, want
 
 
@@ -126,8 +140,8 @@ src, dst, lab = G.directed()
 og = O.Graph.from_edges(G.V, 3, src, dst, lab)
 ctx = fm.Context(prealloc_bytes=1 << 30, soln_prealloc_bytes=64 << 20, output_prealloc_bytes=256 << 20, bank_rows=32)
 g = fm.Graph.from_edges(ctx, G.V, 3, src, dst, lab)
-qs = [S.query_cycle(4, [1, 2, 1, 2]), S.query_clique(4, [1, 2]), S.query_cycle(5, [1, 1, 2, 2, 1]),
-      S.query_clique(5, [2, 1])]
+qs = [S.query_cycle(4, [1, 2, 1, 2]), S.query_clique(4, [1, 2]), S.query_clique(5, [2, 1]),
+      S.query_cycle(4, [1, 1, 2, 2])]
 want = [O.match(og, O.plan(q.to_g_text(), enumerate_aut=0))[0] for q in qs]
 queries = [fm.Query.from_text(q.to_g_text()) for q in qs]
 for engine in (fm.ENGINE_PERSISTENT, fm.ENGINE_LEVELS):
