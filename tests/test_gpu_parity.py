@@ -292,7 +292,7 @@ def test_level_overflow_deferral_gives_identical_results():
     g = fm.Graph.from_edges(small, G.V, 3, src, dst, lab)
     q = S.query_path(5, [1, 2, 1, 2])
     p = O.plan(q.to_g_text(), enumerate_aut=0)
-    oc = O.match(og, p)[0]
+    oc = O.match(og, p, count_rule=True)[0]
     for engine in (fm.ENGINE_PERSISTENT, fm.ENGINE_LEVELS):
         r = fm.match(small, g, fm.Query.from_text(q.to_g_text()), mode=fm.MODE_COUNT, engine=engine)
         assert r.count == oc and r.engine == engine
