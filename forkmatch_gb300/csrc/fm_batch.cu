@@ -216,7 +216,7 @@ template <bool ROOTS>
 __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem& m, uint32_t chunk, uint32_t lane,
                                                 uint32_t d, unsigned long long n_parents, bool& valid,
                                                 uint32_t& k_out, unsigned long long& words, uint32_t sw,
-                                                uint32_t& phase, bool& stage_ok) {
+                                                uint32_t& phase, bool& stage_ok, unsigned long long& rule_cnt) {
     uint32_t qid, pidx;
     if (ROOTS) {
         qid = chunk / P.chunks_per_query;
@@ -233,6 +233,7 @@ __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem
     }
     uint32_t n = 0, drv = 0, k = 0, fin = 0;
     words = 0;
+    rule_cnt = 0;
     if (valid) {
         const BatchPlan& pl = P.plans[qid];
         k = pl.nreq[d];
@@ -256,12 +257,14 @@ __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem
         if (fin && k == 1 && (!P.table_mode || pl.count_only)) {
             // Count rule (the query's count only): every entry of the single
             // list extends the parent except the parent's own vertices, so the
-            // extensions are counted, not enumerated.
+            // extensions are counted, not enumerated.  The caller adds the
+            // count once, when the main pass keeps the chunk (a chunk can be
+            // loaded again after a deferral or for each heavy piece).
             const uint4 sg = m.segs_s[lane];
             unsigned long long c = sg.x;
             for (uint32_t a = 0; a < d; a++)
                 c -= seg_has(sg, m.rows_s[a * 32 + lane], 1, P.nbr, P.bm, P.bm_words) ? 1u : 0u;
-            if (c) atomicAdd(&P.qpos[qid], c);
+            rule_cnt = c;
             n = 0;
         }
     }
@@ -414,9 +417,9 @@ __device__ __forceinline__ void bexpand_main(const BatchParams& P, unsigned char
         }
         bool valid, stage_ok;
         uint32_t k;
-        unsigned long long w;
+        unsigned long long w, rule_cnt;
         const uint32_t total = bload_chunk<ROOTS>(P, m, chunk, lane, d, T.n_parents, valid, k, w, sw, phase,
-                                                  stage_ok);
+                                                  stage_ok, rule_cnt);
         last_chunk = chunk;
         if (!stage_ok) break;
         // only survivors of queries that go on use the next level's buffer;
@@ -443,6 +446,7 @@ __device__ __forceinline__ void bexpand_main(const BatchParams& P, unsigned char
             n_words += w;
             n_parents += 1;
         }
+        if (rule_cnt) atomicAdd(&P.qpos[m.qid_s[lane]], rule_cnt);
         if (total > T.heavy_thresh) {
             int pub = 0;
             const uint32_t np = (total + T.heavy_piece - 1) / T.heavy_piece;
@@ -515,8 +519,8 @@ __device__ __forceinline__ void bexpand_heavy(const BatchParams& P, unsigned cha
         const uint32_t end = min(begin + T.heavy_piece, e.total);
         bool valid, stage_ok;
         uint32_t k;
-        unsigned long long w;
-        bload_chunk<ROOTS>(P, m, e.chunk, lane, d, T.n_parents, valid, k, w, sw, phase, stage_ok);
+        unsigned long long w, rule_cnt;   // counted by the main pass
+        bload_chunk<ROOTS>(P, m, e.chunk, lane, d, T.n_parents, valid, k, w, sw, phase, stage_ok, rule_cnt);
         last_chunk = e.chunk;
         if (!stage_ok) break;
         bprocess<ROOTS>(P, m, e.chunk, begin, end, lane, d, nst);
