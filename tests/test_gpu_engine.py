@@ -178,3 +178,35 @@ def test_staged_membership_lists_give_identical_results(words):
                        timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
     assert "staged ok" in r.stdout
+
+
+def test_count_only_queries_in_a_table_batch(graph):
+    """Queries set to count only in a table-mode batch keep exact counts (the
+    count rule on their last level), get no table region and raise no
+    truncation; the other queries' tables are unchanged."""
+    G, (src, dst, lab), og, texts, want = graph
+    ctx = fm.Context(prealloc_bytes=2 << 30, soln_prealloc_bytes=256 << 20, output_prealloc_bytes=1 << 30,
+                     bank_rows=32)
+    g = fm.Graph.from_edges(ctx, G.V, 3, src, dst, lab)
+    queries = [fm.Query.from_text(t) for t in texts]
+    counted = [w > 1 << 20 for w in want]        # tables too large to keep
+    assert any(counted) and not all(counted)
+    for engine in (fm.ENGINE_PERSISTENT, fm.ENGINE_LEVELS):
+        b = fm.Batch(ctx, g, queries, mode=fm.MODE_TABLE)
+        b.set_engine(engine)
+        for i, c in enumerate(counted):
+            if c:
+                b.set_query_mode(i, fm.MODE_COUNT)
+        for _ in range(2):
+            counts, _ = b.run()
+            assert counts == want
+        for i, (q, w) in enumerate(zip(queries, want)):
+            rows = b.rows(i, max(1, w) if not counted[i] else 1)
+            if counted[i]:
+                assert rows.shape[0] == 0
+            else:
+                c, single, _ = fm.match_table(ctx, g, q, max_rows=max(1, w))
+                assert rows.shape[0] == w and np.array_equal(_sorted(rows), _sorted(single))
+        b.close()
+    g.close()
+    ctx.close()
