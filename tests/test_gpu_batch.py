@@ -107,8 +107,9 @@ def test_batch_each_query_alone_and_in_the_mix(env):
 
 
 def test_batch_level_deferral():
-    """A tiny SOLN_PREALLOC makes shared levels fill: the graph replay reports
-    it and the host drains the deferred chunks; counts must not change."""
+    """A tiny SOLN_PREALLOC makes shared levels fill: the persistent engine
+    drains them on the device, the level-launch engine on the host; counts
+    must not change."""
     G = S.rmat(12, 30000, seed=21, n_elabels=2)
     src, dst, lab = G.directed()
     og = O.Graph.from_edges(G.V, 3, src, dst, lab)
@@ -116,12 +117,17 @@ def test_batch_level_deferral():
                        bank_rows=32)
     g = fm.Graph.from_edges(small, G.V, 3, src, dst, lab)
     qs = [S.query_path(5, [1, 2, 1, 2]), S.query_cycle(4, [1, 1, 2, 2]), S.query_path(4, [2, 2, 1])]
-    want = [O.match(og, O.plan(q.to_g_text(), enumerate_aut=0))[0] for q in qs]
-    b = fm.Batch(small, g, [fm.Query.from_text(q.to_g_text()) for q in qs], mode=fm.MODE_COUNT)
-    counts, st = b.run()
-    assert counts == want
-    assert st.launches > 2 * 4     # deferral relaunched levels
-    b.close()
+    want = [O.match(og, O.plan(q.to_g_text(), enumerate_aut=0), count_rule=True)[0] for q in qs]
+    for engine in (fm.ENGINE_PERSISTENT, fm.ENGINE_LEVELS):
+        b = fm.Batch(small, g, [fm.Query.from_text(q.to_g_text()) for q in qs], mode=fm.MODE_COUNT)
+        b.set_engine(engine)
+        counts, st = b.run()
+        assert counts == want
+        if engine == fm.ENGINE_LEVELS:
+            assert st.launches > 2 * 4     # the host relaunched levels to drain them
+        else:
+            assert st.launches == 2        # the device drained them inside one launch
+        b.close()
     small.close()
 
 

@@ -110,17 +110,22 @@ def test_batch_engines_agree(graph):
                      bank_rows=32)
     g = fm.Graph.from_edges(ctx, G.V, 3, src, dst, lab)
     queries = [fm.Query.from_text(t) for t in texts]
+    tabled = [i for i, w in enumerate(want) if w <= 1 << 20]     # the others are counted only
     for mode in (fm.MODE_COUNT, fm.MODE_TABLE):
         got = {}
         for engine in (fm.ENGINE_PERSISTENT, fm.ENGINE_LEVELS):
             b = fm.Batch(ctx, g, queries, mode=mode)
             b.set_engine(engine)
+            if mode == fm.MODE_TABLE:
+                for i in range(len(queries)):
+                    if i not in tabled:
+                        b.set_query_mode(i, fm.MODE_COUNT)
             for _ in range(2):                 # first run captures, the second replays
                 counts, st = b.run()
                 assert counts == want
                 assert st.persistent == (engine == fm.ENGINE_PERSISTENT)
             if mode == fm.MODE_TABLE:
-                got[engine] = [_sorted(b.rows(i, max(1, want[i]))) for i in range(len(queries))]
+                got[engine] = [_sorted(b.rows(i, max(1, want[i]))) for i in tabled]
             b.close()
         if mode == fm.MODE_TABLE:
             for x, y in zip(got[fm.ENGINE_PERSISTENT], got[fm.ENGINE_LEVELS]):
