@@ -131,11 +131,11 @@ struct BMem {
 };
 
 __host__ __device__ constexpr uint32_t bper_warp_bytes(uint32_t d, uint32_t kmax, uint32_t stage_words = 0) {
-    return 128 * d + 512 * kmax + 6 * 128 + 12 * kBStage + (stage_words ? 16 + 4 * stage_words : 0);
+    return 128 * d + 512 * kmax + 6 * 128 + 12 * kBStage + 4 * stage_words;
 }
 
 __device__ __forceinline__ BMem bmem(unsigned char* smem, uint32_t warp, uint32_t d, uint32_t kmax,
-                                     uint32_t stage_words) {
+                                     uint32_t stage_words, uint64_t* mbar_s) {
     unsigned char* w = smem + warp * bper_warp_bytes(d, kmax, stage_words);
     BMem m;
     m.rows_s = (uint32_t*)w;
@@ -150,8 +150,8 @@ __device__ __forceinline__ BMem bmem(unsigned char* smem, uint32_t warp, uint32_
     m.stp = s + 192;
     m.stx = m.stp + kBStage;
     m.stq = m.stx + kBStage;
-    m.mbar = (uint64_t*)(w + 128 * d + 512 * kmax + 6 * 128 + 12 * kBStage);
-    m.stage = (uint32_t*)(w + 128 * d + 512 * kmax + 6 * 128 + 12 * kBStage + 16);
+    m.mbar = mbar_s + warp;
+    m.stage = (uint32_t*)(w + 128 * d + 512 * kmax + 6 * 128 + 12 * kBStage);
     return m;
 }
 
@@ -387,18 +387,13 @@ __device__ __forceinline__ void bdefer(const BatchParams& P, uint32_t chunk) {
 }
 
 template <bool ROOTS>
-__device__ __forceinline__ void bexpand_main(const BatchParams& P, unsigned char* smem_raw) {
+__device__ __forceinline__ void bexpand_main(const BatchParams& P, unsigned char* smem_raw, uint64_t* mbar_s,
+                                             uint32_t& phase) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t d = P.depth;
     const uint32_t sw = P.kmax >= 2 ? P.stage_words : 0;   // only levels with membership tests stage lists
-    const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax, sw);
+    const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax, sw, mbar_s);
     const BTune T = make_btune(P);
-    uint32_t phase = 0;
-    if (sw) {
-        if (lane == 0) dev::mbar_init(m.mbar, 1);
-        dev::fence_proxy_async_smem();
-        __syncwarp();
-    }
     unsigned long long n_lookups = 0, n_words = 0, n_parents = 0, credit = 0;
     uint32_t nst = 0;
     uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
@@ -485,7 +480,8 @@ __device__ __forceinline__ void bexpand_main(const BatchParams& P, unsigned char
 }
 
 template <bool ROOTS>
-__device__ __forceinline__ void bexpand_heavy(const BatchParams& P, unsigned char* smem_raw) {
+__device__ __forceinline__ void bexpand_heavy(const BatchParams& P, unsigned char* smem_raw, uint64_t* mbar_s,
+                                              uint32_t& phase) {
     const unsigned long long h = *(volatile unsigned long long*)&P.ctl->heavy;
     const uint32_t nent = (uint32_t)(h >> 32);
     const uint32_t npieces = (uint32_t)h;
@@ -493,14 +489,8 @@ __device__ __forceinline__ void bexpand_heavy(const BatchParams& P, unsigned cha
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t d = P.depth;
     const uint32_t sw = P.kmax >= 2 ? P.stage_words : 0;
-    const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax, sw);
+    const BMem m = bmem(smem_raw, threadIdx.x >> 5, d, P.kmax, sw, mbar_s);
     const BTune T = make_btune(P);
-    uint32_t phase = 0;
-    if (sw) {
-        if (lane == 0) dev::mbar_init(m.mbar, 1);
-        dev::fence_proxy_async_smem();
-        __syncwarp();
-    }
     uint32_t nst = 0;
     uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
     for (;;) {
@@ -531,13 +521,19 @@ __device__ __forceinline__ void bexpand_heavy(const BatchParams& P, unsigned cha
 template <bool ROOTS>
 __global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand(const __grid_constant__ BatchParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    bexpand_main<ROOTS>(P, smem_raw);
+    __shared__ uint64_t mbar_s[kBWarps];
+    dev::stage_barriers_init(mbar_s);
+    uint32_t phase = 0;
+    bexpand_main<ROOTS>(P, smem_raw, mbar_s, phase);
 }
 
 template <bool ROOTS>
 __global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand_heavy(const __grid_constant__ BatchParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    bexpand_heavy<ROOTS>(P, smem_raw);
+    __shared__ uint64_t mbar_s[kBWarps];
+    dev::stage_barriers_init(mbar_s);
+    uint32_t phase = 0;
+    bexpand_heavy<ROOTS>(P, smem_raw, mbar_s, phase);
 }
 
 // Persistent batch engine: one cooperative launch runs every level pass of
@@ -559,12 +555,15 @@ __global__ void __launch_bounds__(kBWarps * 32, 5) k_bpersist(const __grid_const
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(16) BatchParams P;
     __shared__ unsigned flag_s, cur_s;
+    __shared__ uint64_t mbar_s[kBWarps];
     SchedState* S = A.sched;
     {
         const uint32_t* src = (const uint32_t*)&P0;
         uint32_t* dst = (uint32_t*)&P;
         for (uint32_t i = threadIdx.x; i < sizeof(BatchParams) / 4; i += blockDim.x) dst[i] = src[i];
     }
+    dev::stage_barriers_init(mbar_s);
+    uint32_t phase = 0;       // of this warp's stage barrier, carried across passes
     bool first = true;
     for (;;) {
         __syncthreads();
@@ -596,12 +595,12 @@ __global__ void __launch_bounds__(kBWarps * 32, 5) k_bpersist(const __grid_const
         __syncthreads();
         const unsigned d = cur_s;
         if (d == 0) break;
-        if (d == 1) bexpand_main<true>(P, smem_raw);
-        else bexpand_main<false>(P, smem_raw);
+        if (d == 1) bexpand_main<true>(P, smem_raw, mbar_s, phase);
+        else bexpand_main<false>(P, smem_raw, mbar_s, phase);
         if (!dev::grid_barrier(S, first && A.hold_first_barrier && blockIdx.x == 0, &flag_s)) break;
         first = false;
-        if (d == 1) bexpand_heavy<true>(P, smem_raw);
-        else bexpand_heavy<false>(P, smem_raw);
+        if (d == 1) bexpand_heavy<true>(P, smem_raw, mbar_s, phase);
+        else bexpand_heavy<false>(P, smem_raw, mbar_s, phase);
         if (!dev::grid_barrier(S, false, &flag_s)) break;
         if (blockIdx.x == 0 && threadIdx.x == 0)
             dev::sched_advance(S, P0.ctl, d, d + 1 < A.maxq, P.n_items, P.ndef_in, P.def_room, false);
@@ -856,7 +855,7 @@ struct BatchRun {
         b->launches += 2;   // the schedule initialisation and the persistent kernel
         const SchedState& h = *cv.h_sched;
         if (h.error & kSchedErrWait) {
-            set_error("a grid-wide wait of the persistent batch kernel ran out");
+            set_error("a bounded wait of the persistent batch kernel ran out (a grid barrier or a list stage)");
             return FM_ERR_DEVICE;
         }
         if (h.error & kSchedErrPasses) {
@@ -935,7 +934,7 @@ struct BatchRun {
             FM_CUDA(cudaStreamSynchronize(s));
             const LaunchCtl c = cv.h_ctl[d];
             if (c.error) {
-                set_error("deferred-chunk list overflow");
+                set_error((c.error & 2u) ? "a list stage's bounded wait ran out" : "deferred-chunk list overflow");
                 return FM_ERR_DEVICE;
             }
             const uint64_t claimed = std::min<uint64_t>(c.claim, items);
@@ -994,7 +993,7 @@ struct BatchRun {
         uint64_t n_parents[kMaxQ] = {};
         for (uint32_t d = 1; d < b->maxq; d++) {
             if (snap[d].error) {
-                set_error("deferred-chunk list overflow");
+                set_error((snap[d].error & 2u) ? "a list stage's bounded wait ran out" : "deferred-chunk list overflow");
                 return FM_ERR_DEVICE;
             }
             n_parents[d] = d == 1 ? (uint64_t)nq * base.chunks_per_query * 32 : snap[d - 1].produced;

@@ -72,6 +72,21 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// Makes mbarrier initialisations visible to the async proxy (the bulk
+// copies' complete_tx) before any copy refers to them.
+__device__ __forceinline__ void fence_mbarrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One completion barrier per warp for the list stage, in static shared memory
+// at a fixed place for the whole launch: initialised once (arrival count 1:
+// lane 0 arms each phase), fenced, then the block synchronises.
+__device__ __forceinline__ void stage_barriers_init(uint64_t* mbar_s) {
+    if ((threadIdx.x & 31) == 0) mbar_init(&mbar_s[threadIdx.x >> 5], 1);
+    fence_mbarrier_init();
+    __syncthreads();
+}
+
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
@@ -243,7 +258,8 @@ __device__ __forceinline__ void sched_advance(SchedState* S, LaunchCtl* ctl_base
     L->produced += produced;
     S->produced_total += produced;
     unsigned err = 0;
-    if (c->error || ndef > def_room) err |= kSchedErrRing;
+    if ((c->error & 1u) || ndef > def_room) err |= kSchedErrRing;
+    if (c->error & 2u) err |= kSchedErrWait;      // a list stage's bounded wait ran out
     const unsigned long long left = sched_remaining(S, d);
     if (mid && produced == 0 && left == items && items > 0) err |= kSchedErrPool;
     if (limit_hit || (S->work_limit && S->produced_total > S->work_limit)) err |= kSchedErrLimit;

@@ -568,7 +568,7 @@ struct MatchRun {
                 res->level[d].kernel_ms += ms;
             }
             if (c.error) {
-                set_error("deferred-chunk list overflow");
+                set_error((c.error & 2u) ? "a list stage's bounded wait ran out" : "deferred-chunk list overflow");
                 return FM_ERR_DEVICE;
             }
         }
@@ -632,7 +632,7 @@ struct MatchRun {
         res->passes += (uint32_t)h.passes;
         res->max_wait_ns = h.wait_seen_ns;
         if (h.error & kSchedErrWait) {
-            set_error("a grid-wide wait of the persistent kernel ran out (wait_limit_ms)");
+            set_error("a bounded wait of the persistent kernel ran out (a grid barrier after wait_limit_ms, or a list stage)");
             return FM_ERR_DEVICE;
         }
         if (h.error & kSchedErrPasses) {
@@ -699,7 +699,7 @@ struct MatchRun {
             }
             add_stats(d, c);
             if (c.error) {
-                set_error("deferred-chunk list overflow");
+                set_error((c.error & 2u) ? "a list stage's bounded wait ran out" : "deferred-chunk list overflow");
                 return FM_ERR_DEVICE;
             }
             if (over_limit()) return FM_ERR_LIMIT;

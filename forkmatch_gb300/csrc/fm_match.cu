@@ -146,11 +146,11 @@ struct WarpMem {
 };
 
 __host__ __device__ constexpr uint32_t per_warp_bytes(uint32_t d, uint32_t k, uint32_t stage_words = 0) {
-    return 128 * d + 512 * k + 256 + 8 * kStage + (stage_words ? 16 + 4 * stage_words : 0);
+    return 128 * d + 512 * k + 256 + 8 * kStage + 4 * stage_words;
 }
 
 __device__ __forceinline__ WarpMem warp_mem(unsigned char* smem_raw, uint32_t warp, uint32_t d, uint32_t k,
-                                            uint32_t stage_words) {
+                                            uint32_t stage_words, uint64_t* mbar_s) {
     unsigned char* ws = smem_raw + warp * per_warp_bytes(d, k, stage_words);
     WarpMem m;
     m.rows_s = (uint32_t*)ws;
@@ -159,8 +159,8 @@ __device__ __forceinline__ WarpMem warp_mem(unsigned char* smem_raw, uint32_t wa
     m.drv_s = m.excl_s + 32;
     m.stp = (uint32_t*)(ws + 128 * d + 512 * k + 256);
     m.stx = m.stp + kStage;
-    m.mbar = (uint64_t*)(ws + 128 * d + 512 * k + 256 + 8 * kStage);
-    m.stage = (uint32_t*)(ws + 128 * d + 512 * k + 256 + 8 * kStage + 16);
+    m.mbar = mbar_s + warp;
+    m.stage = (uint32_t*)(ws + 128 * d + 512 * k + 256 + 8 * kStage);
     return m;
 }
 
@@ -428,20 +428,14 @@ __device__ __forceinline__ bool over_limit(const ExpandParams& P, uint32_t lane,
 // published to the heavy list instead of being walked by one warp.
 template <int MODE, bool ROOTS, bool DUPS>
 __device__ __forceinline__ void expand_main(const ExpandParams& P, unsigned char* smem_raw,
-                                            const uint8_t* col_depth_s) {
+                                            const uint8_t* col_depth_s, uint64_t* mbar_s, uint32_t& phase) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t d = P.depth;
     const uint32_t k = P.plan.nreq[d];
     const uint32_t rb = P.plan.req_begin[d];
     const uint32_t sw = k >= 2 ? P.stage_words : 0;   // only levels with membership tests stage lists
-    const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k, sw);
+    const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k, sw, mbar_s);
     const Tune T = make_tune(P, true);
-    uint32_t phase = 0;
-    if (sw) {
-        if (lane == 0) dev::mbar_init(m.mbar, 1);
-        dev::fence_proxy_async_smem();
-        __syncwarp();
-    }
 
     unsigned long long n_count = 0, n_lookups = 0, n_words = 0, n_parents = 0;
     unsigned long long n_flushed = 0;  // part of n_count already added to tot->count (lane 0)
@@ -578,7 +572,7 @@ __device__ __forceinline__ void expand_main(const ExpandParams& P, unsigned char
 // main pass already holds the chunk's output budget and counted its work.
 template <int MODE, bool ROOTS, bool DUPS>
 __device__ __forceinline__ void expand_heavy(const ExpandParams& P, unsigned char* smem_raw,
-                                             const uint8_t* col_depth_s) {
+                                             const uint8_t* col_depth_s, uint64_t* mbar_s, uint32_t& phase) {
     const unsigned long long h = *(volatile unsigned long long*)&P.ctl->heavy;
     const uint32_t nent = (uint32_t)(h >> 32);
     const uint32_t npieces = (uint32_t)h;
@@ -588,14 +582,8 @@ __device__ __forceinline__ void expand_heavy(const ExpandParams& P, unsigned cha
     const uint32_t k = P.plan.nreq[d];
     const uint32_t rb = P.plan.req_begin[d];
     const uint32_t sw = k >= 2 ? P.stage_words : 0;
-    const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k, sw);
+    const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k, sw, mbar_s);
     const Tune T = make_tune(P, false);
-    uint32_t phase = 0;
-    if (sw) {
-        if (lane == 0) dev::mbar_init(m.mbar, 1);
-        dev::fence_proxy_async_smem();
-        __syncwarp();
-    }
     unsigned long long n_count = 0, n_flushed = 0;
     uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
     uint32_t nst = 0;
@@ -629,18 +617,22 @@ template <int MODE, bool ROOTS, bool DUPS>
 __global__ void __launch_bounds__(kWarps * 32, 6) k_expand(const __grid_constant__ ExpandParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint8_t col_depth_s[kMaxQ];
+    __shared__ uint64_t mbar_s[kWarps];
     if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P.plan.col_depth[threadIdx.x];
-    __syncthreads();
-    expand_main<MODE, ROOTS, DUPS>(P, smem_raw, col_depth_s);
+    dev::stage_barriers_init(mbar_s);
+    uint32_t phase = 0;
+    expand_main<MODE, ROOTS, DUPS>(P, smem_raw, col_depth_s, mbar_s, phase);
 }
 
 template <int MODE, bool ROOTS, bool DUPS>
 __global__ void __launch_bounds__(kWarps * 32, 6) k_expand_heavy(const __grid_constant__ ExpandParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint8_t col_depth_s[kMaxQ];
+    __shared__ uint64_t mbar_s[kWarps];
     if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P.plan.col_depth[threadIdx.x];
-    __syncthreads();
-    expand_heavy<MODE, ROOTS, DUPS>(P, smem_raw, col_depth_s);
+    dev::stage_barriers_init(mbar_s);
+    uint32_t phase = 0;
+    expand_heavy<MODE, ROOTS, DUPS>(P, smem_raw, col_depth_s, mbar_s, phase);
 }
 
 // ------------------------------------------------------- persistent engine
@@ -656,25 +648,25 @@ __global__ void __launch_bounds__(kWarps * 32, 6) k_expand_heavy(const __grid_co
 
 template <int LAST, bool DUPS>
 __device__ __forceinline__ void persist_main(const ExpandParams& P, unsigned char* smem, const uint8_t* cd,
-                                             bool roots, bool last) {
+                                             bool roots, bool last, uint64_t* mb, uint32_t& ph) {
     if (last) {
-        if (roots) expand_main<LAST, true, DUPS>(P, smem, cd);
-        else expand_main<LAST, false, DUPS>(P, smem, cd);
+        if (roots) expand_main<LAST, true, DUPS>(P, smem, cd, mb, ph);
+        else expand_main<LAST, false, DUPS>(P, smem, cd, mb, ph);
     } else {
-        if (roots) expand_main<kModeMid, true, DUPS>(P, smem, cd);
-        else expand_main<kModeMid, false, DUPS>(P, smem, cd);
+        if (roots) expand_main<kModeMid, true, DUPS>(P, smem, cd, mb, ph);
+        else expand_main<kModeMid, false, DUPS>(P, smem, cd, mb, ph);
     }
 }
 
 template <int LAST, bool DUPS>
 __device__ __forceinline__ void persist_heavy(const ExpandParams& P, unsigned char* smem, const uint8_t* cd,
-                                              bool roots, bool last) {
+                                              bool roots, bool last, uint64_t* mb, uint32_t& ph) {
     if (last) {
-        if (roots) expand_heavy<LAST, true, DUPS>(P, smem, cd);
-        else expand_heavy<LAST, false, DUPS>(P, smem, cd);
+        if (roots) expand_heavy<LAST, true, DUPS>(P, smem, cd, mb, ph);
+        else expand_heavy<LAST, false, DUPS>(P, smem, cd, mb, ph);
     } else {
-        if (roots) expand_heavy<kModeMid, true, DUPS>(P, smem, cd);
-        else expand_heavy<kModeMid, false, DUPS>(P, smem, cd);
+        if (roots) expand_heavy<kModeMid, true, DUPS>(P, smem, cd, mb, ph);
+        else expand_heavy<kModeMid, false, DUPS>(P, smem, cd, mb, ph);
     }
 }
 
@@ -685,6 +677,7 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_persist(const __grid_constan
     __shared__ __align__(16) ExpandParams P;          // level fields change per pass
     __shared__ uint8_t col_depth_s[kMaxQ];
     __shared__ unsigned flag_s, cur_s;
+    __shared__ uint64_t mbar_s[kWarps];
     SchedState* S = A.sched;
     {
         const uint32_t* src = (const uint32_t*)&P0;
@@ -692,6 +685,8 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_persist(const __grid_constan
         for (uint32_t i = threadIdx.x; i < sizeof(ExpandParams) / 4; i += blockDim.x) dst[i] = src[i];
     }
     if (threadIdx.x < (unsigned)kMaxQ) col_depth_s[threadIdx.x] = P0.plan.col_depth[threadIdx.x];
+    dev::stage_barriers_init(mbar_s);
+    uint32_t phase = 0;       // of this warp's stage barrier, carried across passes
     const uint32_t q = P0.plan.q;
     bool first = true;
     for (;;) {
@@ -724,10 +719,10 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_persist(const __grid_constan
         const unsigned d = cur_s;
         if (d == 0) break;
         const bool roots = d == 1, last = d + 1 == q;
-        persist_main<LAST, DUPS>(P, smem_raw, col_depth_s, roots, last);
+        persist_main<LAST, DUPS>(P, smem_raw, col_depth_s, roots, last, mbar_s, phase);
         if (!dev::grid_barrier(S, first && A.hold_first_barrier && blockIdx.x == 0, &flag_s)) break;
         first = false;
-        persist_heavy<LAST, DUPS>(P, smem_raw, col_depth_s, roots, last);
+        persist_heavy<LAST, DUPS>(P, smem_raw, col_depth_s, roots, last, mbar_s, phase);
         if (!dev::grid_barrier(S, false, &flag_s)) break;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             const bool limit_hit = P.work_limit && (*(volatile unsigned*)&P.tot->error & kLimitFlag);
