@@ -262,8 +262,12 @@ __device__ __forceinline__ void sched_advance(SchedState* S, LaunchCtl* ctl_base
     if (c->error & 2u) err |= kSchedErrWait;      // a list stage's bounded wait ran out
     const unsigned long long left = sched_remaining(S, d);
     if (mid && produced == 0 && left == items && items > 0) err |= kSchedErrPool;
-    if (limit_hit || (S->work_limit && S->produced_total > S->work_limit)) err |= kSchedErrLimit;
+    if (limit_hit) err |= kSchedErrLimit;
     if (S->passes > kSchedMaxPasses) err |= kSchedErrPasses;
+    // Past the work limit on partial matches, the rows already produced are
+    // still carried down to the last level (whose own limit check stops the
+    // count), but no level is resumed: the result is a lower bound.
+    const bool over = S->work_limit && S->produced_total > S->work_limit;
     unsigned next = 0;
     if (!err) {
         if (mid && produced > 0) {
@@ -273,6 +277,8 @@ __device__ __forceinline__ void sched_advance(SchedState* S, LaunchCtl* ctl_base
             N->fresh = 0;
             N->head = 0;
             N->tail = 0;
+        } else if (over) {
+            err |= kSchedErrLimit;
         } else {
             next = d;
             while (next >= 1 && sched_remaining(S, next) == 0) next--;
