@@ -23,7 +23,7 @@ FM_ERR_LIMIT = 16
 MODE_TABLE, MODE_COUNT = 0, 1
 COLUMNS_REFERENCE, COLUMNS_QUERY_ID = 0, 1
 ORDER_AUTO, ORDER_REFERENCE = 0, 1
-ENGINE_PERSISTENT, ENGINE_LEVELS = 0, 1
+ENGINE_LEVELS, ENGINE_PERSISTENT = 0, 1
 
 STATUS_NAMES = {
     0: "FM_OK", 1: "FM_ERR_ARG", 2: "FM_ERR_IO", 3: "FM_ERR_DATA_HEADER0", 4: "FM_ERR_DATA_TRAILER",
@@ -323,16 +323,16 @@ class PinnedRows:
 
 def match(ctx, graph, query, mode=MODE_TABLE, columns=COLUMNS_REFERENCE, host_rows=None, roots=None,
           profile=False, stream=None, allow_truncation=False, order=ORDER_AUTO, host_direct=False, work_limit=0,
-          allow_limit=False, engine=ENGINE_PERSISTENT, wait_limit_ms=0, test_stall_barrier=False,
+          allow_limit=False, engine=ENGINE_LEVELS, wait_limit_ms=0, test_stall_barrier=False,
           allow_device_error=False):
     """Run fm_match.  Returns the Result struct; with ``host_rows`` (a
     PinnedRows or a C-contiguous uint32 numpy array) the table is copied there.
     ``host_direct`` (PinnedRows only): the kernels write the table straight
     into the pinned host buffer instead of device memory.  ``work_limit``:
     stop after that many embeddings or partial matches (FM_ERR_LIMIT, raised
-    unless ``allow_limit``).  ``engine``: ENGINE_PERSISTENT (one cooperative
-    launch, passes scheduled on the device) or ENGINE_LEVELS (launch pairs per
-    pass, drains scheduled by the host)."""
+    unless ``allow_limit``).  ``engine``: ENGINE_LEVELS (launch pairs per
+    pass, drains scheduled by the host; the default) or ENGINE_PERSISTENT (one
+    cooperative launch, passes scheduled on the device)."""
     o = MatchOpts()
     lib().fm_match_opts_default(ctypes.byref(o))
     o.mode = mode

@@ -93,6 +93,7 @@ constexpr uint32_t kHeavyMaxPieces = 65536;
 struct BTune {
     unsigned long long n_parents, n_items;
     uint32_t credit_block, heavy_thresh, heavy_piece;
+    uint32_t claim_batch;    // chunks claimed per atomic (a level of 10^9 chunks must not serialise on one counter)
 };
 
 __device__ __forceinline__ BTune make_btune(const BatchParams& P) {
@@ -110,6 +111,11 @@ __device__ __forceinline__ BTune make_btune(const BatchParams& P) {
     const uint32_t base = t.n_items >= 4 * all_warps ? 2048u : (t.n_items >= all_warps ? 512u : 128u);
     t.heavy_piece = base << P.piece_shift;
     t.heavy_thresh = 2 * t.heavy_piece;
+    // roots cost about the same per chunk: big batches; deeper chunks vary:
+    // small batches keep the warps balanced
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
+    const unsigned long long b = (t.n_items / warps + 1) / (P.pin ? 16 : 2);
+    t.claim_batch = (uint32_t)(b < 1 ? 1 : (b > 8 ? 8 : b));
     return t;
 }
 
@@ -397,73 +403,94 @@ __device__ __forceinline__ void bexpand_main(const BatchParams& P, unsigned char
     unsigned long long n_lookups = 0, n_words = 0, n_parents = 0, credit = 0;
     uint32_t nst = 0;
     uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
-    for (;;) {
-        unsigned long long item = 0;
-        if (lane == 0) item = atomicAdd(&P.ctl->claim, 1ull);
-        item = __shfl_sync(kFull, item, 0);
-        if (item >= T.n_items) break;
-        const uint32_t chunk = bitem_chunk(P, item);
-        int stop = 0;
-        if (lane == 0) stop = *(volatile unsigned int*)&P.ctl->stop ? 1 : 0;
-        stop = __shfl_sync(kFull, stop, 0);
-        if (stop) {
-            if (lane == 0) bdefer(P, chunk);
-            break;
-        }
-        bool valid, stage_ok;
-        uint32_t k;
-        unsigned long long w, rule_cnt;
-        const uint32_t total = bload_chunk<ROOTS>(P, m, chunk, lane, d, T.n_parents, valid, k, w, sw, phase,
-                                                  stage_ok, rule_cnt);
-        last_chunk = chunk;
-        if (!stage_ok) break;
-        // only survivors of queries that go on use the next level's buffer;
-        // the upper bound of the whole chunk is reserved (over-reserving is safe)
-        if (total && P.pout) {
-            int ok = 1;
-            if (lane == 0 && total > credit) {
-                const unsigned long long need = max((unsigned long long)total, (unsigned long long)T.credit_block);
-                const unsigned long long old = atomicAdd(&P.ctl->budget, need);
-                if (old + need > P.ocap) {
-                    ok = 0;
-                    atomicExch(&P.ctl->stop, 1u);
-                    bdefer(P, chunk);
-                } else {
-                    credit += need;
+    bool done = false;
+    while (!done) {
+        unsigned long long first = 0;
+        if (lane == 0) first = atomicAdd(&P.ctl->claim, (unsigned long long)T.claim_batch);
+        first = __shfl_sync(kFull, first, 0);
+        if (first >= T.n_items) break;
+        const unsigned long long last = first + T.claim_batch < T.n_items ? first + T.claim_batch : T.n_items;
+        for (unsigned long long item = first; item < last; item++) {
+            const uint32_t chunk = bitem_chunk(P, item);
+            int stop = 0;
+            if (lane == 0) stop = *(volatile unsigned int*)&P.ctl->stop ? 1 : 0;
+            stop = __shfl_sync(kFull, stop, 0);
+            if (stop) {
+                if (lane == 0)
+                    for (unsigned long long it = item; it < last; it++) bdefer(P, bitem_chunk(P, it));
+                done = true;
+                break;
+            }
+            bool valid, stage_ok;
+            uint32_t k;
+            unsigned long long w, rule_cnt;
+            const uint32_t total = bload_chunk<ROOTS>(P, m, chunk, lane, d, T.n_parents, valid, k, w, sw, phase,
+                                                      stage_ok, rule_cnt);
+            last_chunk = chunk;
+            if (!stage_ok) {
+                done = true;
+                break;
+            }
+            // only survivors of queries that go on use the next level's buffer;
+            // the upper bound of the whole chunk is reserved (over-reserving is safe)
+            if (total && P.pout) {
+                int ok = 1;
+                if (lane == 0 && total > credit) {
+                    const unsigned long long need =
+                        max((unsigned long long)total, (unsigned long long)T.credit_block);
+                    const unsigned long long old = atomicAdd(&P.ctl->budget, need);
+                    if (old + need > P.ocap) {
+                        ok = 0;
+                        atomicExch(&P.ctl->stop, 1u);
+                        for (unsigned long long it = item; it < last; it++) bdefer(P, bitem_chunk(P, it));
+                    } else {
+                        credit += need;
+                    }
+                }
+                if (lane == 0 && ok) credit -= total;
+                ok = __shfl_sync(kFull, ok, 0);
+                if (!ok) {
+                    done = true;
+                    break;
                 }
             }
-            if (lane == 0 && ok) credit -= total;
-            ok = __shfl_sync(kFull, ok, 0);
-            if (!ok) break;
-        }
-        if (valid) {
-            n_lookups += k;
-            n_words += w;
-            n_parents += 1;
-        }
-        if (rule_cnt) atomicAdd(&P.qpos[m.qid_s[lane]], rule_cnt);
-        if (total > T.heavy_thresh) {
-            int pub = 0;
-            const uint32_t np = (total + T.heavy_piece - 1) / T.heavy_piece;
-            if (lane == 0 && np <= kHeavyMaxPieces) {
-                const unsigned long long h = *(volatile unsigned long long*)&P.ctl->heavy;
-                if ((uint32_t)(h >> 32) + P.max_warps < P.heavy_cap && (uint32_t)h < (1u << 31)) {
-                    const unsigned long long old = atomicAdd(&P.ctl->heavy, (1ull << 32) | np);
-                    HeavyEntry e;
-                    e.chunk = chunk;
-                    e.total = total;
-                    e.piece0 = (uint32_t)old;
-                    e.pieces = np;
-                    P.heavy[(uint32_t)(old >> 32)] = e;
-                    pub = 1;
-                }
+            if (valid) {
+                n_lookups += k;
+                n_words += w;
+                n_parents += 1;
             }
-            pub = __shfl_sync(kFull, pub, 0);
-            if (pub) continue;
+            {
+                // count-rule counts: one atomic per query present in the chunk
+                // (each lane's count is below 2^27, a warp's sum below 2^32)
+                const uint32_t key = rule_cnt ? m.qid_s[lane] : 0xffffffffu;
+                const unsigned grp = __match_any_sync(kFull, key);
+                const unsigned sum = __reduce_add_sync(grp, (unsigned)rule_cnt);
+                if (key != 0xffffffffu && (int)lane == __ffs(grp) - 1)
+                    atomicAdd(&P.qpos[key], (unsigned long long)sum);
+            }
+            if (total > T.heavy_thresh) {
+                int pub = 0;
+                const uint32_t np = (total + T.heavy_piece - 1) / T.heavy_piece;
+                if (lane == 0 && np <= kHeavyMaxPieces) {
+                    const unsigned long long h = *(volatile unsigned long long*)&P.ctl->heavy;
+                    if ((uint32_t)(h >> 32) + P.max_warps < P.heavy_cap && (uint32_t)h < (1u << 31)) {
+                        const unsigned long long old = atomicAdd(&P.ctl->heavy, (1ull << 32) | np);
+                        HeavyEntry e;
+                        e.chunk = chunk;
+                        e.total = total;
+                        e.piece0 = (uint32_t)old;
+                        e.pieces = np;
+                        P.heavy[(uint32_t)(old >> 32)] = e;
+                        pub = 1;
+                    }
+                }
+                pub = __shfl_sync(kFull, pub, 0);
+                if (pub) continue;
+            }
+            bprocess<ROOTS>(P, m, chunk, 0, total, lane, d, nst);
+            // the stage refers to this chunk's query ids only through stq, and to
+            // its parents through pidx: it can outlive the chunk
         }
-        bprocess<ROOTS>(P, m, chunk, 0, total, lane, d, nst);
-        // the stage refers to this chunk's query ids only through stq, and to
-        // its parents through pidx: it can outlive the chunk
     }
     if (nst) bflush<ROOTS>(P, m, nst, lane, d, last_chunk);
 #pragma unroll
@@ -698,7 +725,7 @@ struct fm_batch {
     }
     uint32_t piece_shift = 0;
     uint32_t sm_fraction = 4;             // quarters of the full grid used by the main pass
-    bool persistent = true;               // one cooperative launch per run (else level launches)
+    bool persistent = false;              // one cooperative launch per run (else level launches)
     bool graph_ok = true;                 // capture of the run succeeded (else launched directly)
     uint64_t cap_full = 0;                // largest level buffer (rows) SOLN_PREALLOC allows
     uint64_t cap_floor = 0;               // smallest level buffer one chunk per level needs
@@ -1042,6 +1069,10 @@ fm_status batch_create_impl(fm_context* ctx, const fm_graph* graph, const fm_que
         return FM_ERR_ARG;
     }
     FM_CUDA(cudaSetDevice(cv.device));
+    if ((uint64_t)g.max_len * 32 >= (1ull << 32)) {
+        set_error("a neighbour list is longer than 2^27");
+        return FM_ERR_UNSUPPORTED;
+    }
     std::vector<BatchPlan> plans;
     uint64_t table_words = 0;
     for (uint32_t i = 0; i < n; i++) {
@@ -1367,34 +1398,37 @@ fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
     // depth-first drain in L2, large ones need fewer passes); keep the
     // fastest.  Each configuration runs the whole batch twice (capture, then
     // the timed replay).
-    const uint32_t shifts[] = {0, 1};
-    const uint32_t quarters[] = {2, 4};
-    const uint32_t banks[] = {0, 4, 8};
+    // Candidates: both engines at the full grid and full level buffers, then
+    // for the level engine the split granularity, a half grid and smaller
+    // level buffers.  Each candidate runs the whole batch once (capturing its
+    // graph, which the run then launches) and is timed on that run.
+    struct Cand {
+        bool persistent;
+        uint32_t shift, quarters, bank;
+    };
+    std::vector<Cand> cands = {{false, 0, 4, 0}, {true, 0, 4, 0}, {false, 1, 4, 0}, {false, 0, 2, 0},
+                               {false, 0, 4, 4}, {false, 0, 4, 8}};
+    if (!b->replay) cands.erase(cands.begin() + 1);   // a server's batches use level launches
     double best_ms = -1;
-    uint32_t bs = b->piece_shift, bq = b->sm_fraction, bb = b->bank_shift;
-    for (uint32_t bank : banks) {
-        if (bank && (b->cap_full >> bank) < b->cap_floor) continue;
-        for (uint32_t sh : shifts) {
-            for (uint32_t qu : quarters) {
-                b->piece_shift = sh;
-                b->sm_fraction = qu;
-                b->bank_shift = bank;
-                b->layout_levels(b->cap_full >> bank);
-                b->drop_graphs();
-                fm_batch_stats st;
-                fm_status s = fm_batch_run(b, nullptr, &st);   // builds the graph
-                if (s != FM_OK && s != FM_ERR_OUTPUT_OVERFLOW) return s;
-                s = fm_batch_run(b, nullptr, &st);             // timed replay
-                if (s != FM_OK && s != FM_ERR_OUTPUT_OVERFLOW) return s;
-                if (best_ms < 0 || st.wall_ms < best_ms) {
-                    best_ms = st.wall_ms;
-                    bs = sh;
-                    bq = qu;
-                    bb = bank;
-                }
-            }
+    Cand best_c = {b->persistent, b->piece_shift, b->sm_fraction, b->bank_shift};
+    for (const Cand& c : cands) {
+        if (c.bank && (b->cap_full >> c.bank) < b->cap_floor) continue;
+        b->persistent = c.persistent;
+        b->piece_shift = c.shift;
+        b->sm_fraction = c.quarters;
+        b->bank_shift = c.bank;
+        b->layout_levels(b->cap_full >> c.bank);
+        b->drop_graphs();
+        fm_batch_stats st;
+        fm_status s = fm_batch_run(b, nullptr, &st);
+        if (s != FM_OK && s != FM_ERR_OUTPUT_OVERFLOW) return s;
+        if (best_ms < 0 || st.wall_ms < best_ms) {
+            best_ms = st.wall_ms;
+            best_c = c;
         }
     }
+    b->persistent = best_c.persistent;
+    const uint32_t bs = best_c.shift, bq = best_c.quarters, bb = best_c.bank;
     b->piece_shift = bs;
     b->sm_fraction = bq;
     b->bank_shift = bb;

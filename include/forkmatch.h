@@ -179,7 +179,8 @@ typedef struct fm_match_opts {
     uint64_t work_limit;        /* 0: none.  Otherwise stop once more than this many embeddings
                                    were counted, or partial matches produced, and return
                                    FM_ERR_LIMIT (count and rows are then a lower bound) */
-    int32_t engine;             /* fm_engine; profile = 1 always uses FM_ENGINE_LEVELS */
+    int32_t engine;             /* fm_engine (default FM_ENGINE_LEVELS); profile = 1 always uses
+                                   FM_ENGINE_LEVELS */
     uint32_t wait_limit_ms;     /* persistent engine: bound on one grid-wide wait between level
                                    passes (0: 60000).  A wait that runs out ends the match with
                                    FM_ERR_DEVICE; the context stays usable */
@@ -190,16 +191,18 @@ typedef struct fm_match_opts {
 /* How the level passes of a match are driven.  Both replace the reference's
  * dynamic-parallelism forks (src/smsm.cu:564-687, 949-1139) and give the same
  * results.
+ *   FM_ENGINE_LEVELS (default): one main + heavy launch pair per level pass,
+ *     launched back to back; a level whose output buffer filled is drained by
+ *     the host, depth first.  Measured faster on GB300 (fewer grid-wide
+ *     synchronisations per pass, higher occupancy).
  *   FM_ENGINE_PERSISTENT: one cooperative launch per match.  Each depth has a
  *     device work queue (a ring of chunks pushed back when the output level
  *     filled, then the fresh chunks); the kernel schedules the passes depth
  *     first on the device, and warps that finish their own chunks take pieces
- *     of long (hub) chunks.  No host round trip between passes.
- *   FM_ENGINE_LEVELS: one main + heavy launch pair per level pass; a level
- *     whose output buffer filled is drained by the host, depth first. */
+ *     of long (hub) chunks.  No host round trip between passes. */
 typedef enum fm_engine {
-    FM_ENGINE_PERSISTENT = 0,
-    FM_ENGINE_LEVELS = 1
+    FM_ENGINE_LEVELS = 0,
+    FM_ENGINE_PERSISTENT = 1
 } fm_engine;
 
 /* Matching order.  Results (count, row set, column layout) do not depend on
@@ -245,10 +248,10 @@ fm_status fm_match(fm_context* ctx, const fm_graph* g, const fm_query* q,
 /* Batched matching.  No counterpart in the reference, which matches one query
  * per program run (src/smsm.cu:1182-1349): a batch matches many compiled
  * queries against one resident graph in shared level passes, each query's
- * results identical to fm_match's.  A run is one persistent cooperative
- * launch fed by per-depth work queues (FM_ENGINE_PERSISTENT), captured once as
- * a CUDA graph and replayed; where that launch does not fit, max(q) - 1 level
- * launch pairs.  In table mode the first run counts every query
+ * results identical to fm_match's: max(q) - 1 level launch pairs
+ * (FM_ENGINE_LEVELS) or one persistent cooperative launch fed by per-depth
+ * work queues (FM_ENGINE_PERSISTENT), captured once as a CUDA graph and
+ * replayed.  In table mode the first run counts every query
  * (a counting replay) and then gives each one a table region of exactly its
  * size in OUTPUT_PREALLOC, in batch order while it lasts (a query that does
  * not fit gets FM_ERR_OUTPUT_OVERFLOW; counts stay exact).  Queries with one
@@ -288,12 +291,12 @@ fm_status fm_batch_copy_tables(const fm_batch* b, uint32_t* host, uint64_t cap_w
  * mode a last depth with a single back edge is counted from the list (length
  * minus the vertices already matched) instead of enumerated. */
 fm_status fm_batch_set_query_mode(fm_batch* b, uint32_t i, int32_t mode);
-/* Engine of later runs (fm_engine; default FM_ENGINE_PERSISTENT).  Results
- * do not depend on it. */
+/* Engine of later runs (fm_engine; default FM_ENGINE_LEVELS, and
+ * fm_batch_tune picks the faster one).  Results do not depend on it. */
 fm_status fm_batch_set_engine(fm_batch* b, int32_t engine);
-/* Autotuner: runs the batch under each candidate split granularity (the
- * intersection tile a warp walks), grid (warps in flight per SM) and level
- * buffer size (the bank size), keeps the fastest for later runs. */
+/* Autotuner: runs the batch under each candidate engine, split granularity
+ * (the intersection tile a warp walks), grid (warps in flight per SM) and
+ * level buffer size (the bank size), keeps the fastest for later runs. */
 fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best);
 void fm_batch_free(fm_batch* b);
 
