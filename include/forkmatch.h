@@ -179,8 +179,8 @@ typedef struct fm_match_opts {
     uint64_t work_limit;        /* 0: none.  Otherwise stop once more than this many embeddings
                                    were counted, or partial matches produced, and return
                                    FM_ERR_LIMIT (count and rows are then a lower bound) */
-    int32_t engine;             /* fm_engine (default FM_ENGINE_LEVELS); profile = 1 always uses
-                                   FM_ENGINE_LEVELS */
+    int32_t engine;             /* an fm_engine value, FM_ENGINE_LEVELS by default; profile = 1
+                                   always uses FM_ENGINE_LEVELS */
     uint32_t wait_limit_ms;     /* persistent engine: bound on one grid-wide wait between level
                                    passes (0: 60000).  A wait that runs out ends the match with
                                    FM_ERR_DEVICE; the context stays usable */
@@ -291,8 +291,8 @@ fm_status fm_batch_copy_tables(const fm_batch* b, uint32_t* host, uint64_t cap_w
  * mode a last depth with a single back edge is counted from the list (length
  * minus the vertices already matched) instead of enumerated. */
 fm_status fm_batch_set_query_mode(fm_batch* b, uint32_t i, int32_t mode);
-/* Engine of later runs (fm_engine; default FM_ENGINE_LEVELS, and
- * fm_batch_tune picks the faster one).  Results do not depend on it. */
+/* Engine of later runs: an fm_engine value, FM_ENGINE_LEVELS by default;
+ * fm_batch_tune picks the faster one.  Results do not depend on it. */
 fm_status fm_batch_set_engine(fm_batch* b, int32_t engine);
 /* Autotuner: runs the batch under each candidate engine, split granularity
  * (the intersection tile a warp walks), grid (warps in flight per SM) and
