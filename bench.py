@@ -97,7 +97,7 @@ def run_ncu_step(args):
     wl, G, (src, dst, lab), same, _ = load_workload(args.workload)
     pick = None if args.queries == "all" else {int(x) for x in args.queries.split(",")}
     # the table region only as large as the picked table queries need
-    need = sum(q["count"] * q["k"] * 4 for i, q in enumerate(wl["queries"])
+    need = sum(q["count"] * query_vertices(q) * 4 for i, q in enumerate(wl["queries"])
                if (pick is None or i in pick) and not is_count_only(q))
     out_bytes = min(int(4.5 * GB), ((need + (64 << 20)) >> 20) << 20)
     ctx = fm.Context(prealloc_bytes=2 * GB + out_bytes + (128 << 20), soln_prealloc_bytes=2 * GB,
@@ -265,6 +265,11 @@ CPU_EVERY = {"batched": 32, "plain_at_scale": 1}
 
 def oracle_sample(wl, every):
     return [i for i in range(len(wl["queries"])) if i % every == 0]
+
+
+def query_vertices(qm):
+    """Vertices of a recorded query (the first field of its .g header line)."""
+    return int(qm["text"].split("\n")[1].split()[0])
 
 
 def is_count_only(qm):
@@ -759,7 +764,8 @@ def run_batched(args, rank, world, local):
             "rows_equal_sample": {"queries": len(sample), "equal": rows_ok},
             "tuned": {"engine": "persistent" if st.persistent else "levels",
                       "piece_shift": tune.piece_shift, "grid_quarters": tune.grid_quarters,
-                      "level_rows": tune.level_rows, "persistent": bool(st.persistent), "graph": bool(st.graph),
+                      "level_rows": tune.level_rows, "weighted_levels": bool(st.weighted_levels),
+                      "persistent": bool(st.persistent), "graph": bool(st.graph),
                       "batched_queries": st.batched_queries, "single_queries": st.single_queries},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": batched_traffic(alg_bytes / max(1, world)),

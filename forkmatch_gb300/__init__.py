@@ -95,7 +95,8 @@ class BatchStats(ctypes.Structure):
     _fields_ = [("embeddings", ctypes.c_uint64), ("launches", ctypes.c_uint64), ("wall_ms", ctypes.c_double),
                 ("batched_queries", ctypes.c_uint32), ("single_queries", ctypes.c_uint32),
                 ("piece_shift", ctypes.c_uint32), ("grid_quarters", ctypes.c_uint32),
-                ("level_rows", ctypes.c_uint64), ("persistent", ctypes.c_int32), ("graph", ctypes.c_int32)]
+                ("level_rows", ctypes.c_uint64), ("persistent", ctypes.c_int32), ("graph", ctypes.c_int32),
+                ("weighted_levels", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class ServerOpts(ctypes.Structure):

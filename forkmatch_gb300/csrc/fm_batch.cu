@@ -570,6 +570,7 @@ __global__ void __launch_bounds__(kBWarps * 32, 6) k_bexpand_heavy(const __grid_
 struct BatchPersistArgs {
     SchedState* sched;
     uint32_t* levels[kMaxQ];
+    uint64_t caps[kMaxQ];             // rows of each level buffer
     uint32_t kmax[kMaxQ];
     uint32_t* rings;
     uint32_t ring_cap;
@@ -606,6 +607,8 @@ __global__ void __launch_bounds__(kBWarps * 32, 5) k_bpersist(const __grid_const
                 P.kmax = A.kmax[d];
                 P.pin = d == 1 ? nullptr : A.levels[d];
                 P.pout = d + 1 < A.maxq ? A.levels[d + 1] : nullptr;
+                P.pstride = d >= 2 ? A.caps[d] : 0;
+                P.ocap = d + 1 < A.maxq ? A.caps[d + 1] : 0;
                 P.n_parents = L->n_parents;
                 P.ndef_in = (uint32_t)ring;
                 P.fresh_base = L->fresh;
@@ -732,14 +735,64 @@ struct fm_batch {
     uint32_t bank_shift = 0;              // tuned: level buffers of cap_full >> bank_shift rows
     char* soln = nullptr;
 
+    uint64_t lcap[kMaxQ] = {};            // rows of the level buffer of depth d (d >= 2)
+    uint64_t vol[kMaxQ] = {};             // rows that passed through level d in the last run
+    bool weighted = false;                // level buffers sized from `vol` (else all equal)
+
     // Level buffers of `cap` rows each, packed from the start of the level region.
     void layout_levels(uint64_t cap) {
+        weighted = false;
         level_cap = cap;
         uint64_t loff = 0;
         for (uint32_t d = 2; d < maxq; d++) {
+            lcap[d] = cap;
             level[d] = (uint32_t*)(soln + loff);
             loff += 4ull * (d + 1) * cap;
         }
+    }
+
+    // Level buffers sized from the last run's per-depth volumes: a depth gets
+    // room for all its rows when everything fits, else water-filling gives
+    // every depth min(its volume, C) rows (never below one chunk's worth),
+    // with C as large as SOLN_PREALLOC allows.  A batch whose queries stress
+    // one depth (long paths) then drains it a few times instead of splitting
+    // the memory evenly over every depth.  Returns false without volumes.
+    bool layout_weighted() {
+        uint64_t want[kMaxQ] = {};
+        bool any = false;
+        for (uint32_t d = 2; d < maxq; d++) {
+            want[d] = std::max<uint64_t>(vol[d], cap_floor);
+            any = any || vol[d] > 0;
+        }
+        if (!any) return false;
+        const uint64_t budget = cap_full * ([&] {
+            uint64_t c = 0;
+            for (uint32_t d = 2; d < maxq; d++) c += 4ull * (d + 1);
+            return c;
+        }());
+        auto bytes_at = [&](uint64_t C) {
+            uint64_t t = 0;
+            for (uint32_t d = 2; d < maxq; d++) t += 4ull * (d + 1) * std::max(cap_floor, std::min(want[d], C));
+            return t;
+        };
+        uint64_t lo = cap_floor, hi = 0;
+        for (uint32_t d = 2; d < maxq; d++) hi = std::max(hi, want[d]);
+        if (bytes_at(lo) > budget) return false;
+        while (lo < hi) {                      // largest C whose layout fits
+            const uint64_t mid = lo + (hi - lo + 1) / 2;
+            if (bytes_at(mid) <= budget) lo = mid;
+            else hi = mid - 1;
+        }
+        weighted = true;
+        uint64_t loff = 0;
+        level_cap = 0;
+        for (uint32_t d = 2; d < maxq; d++) {
+            lcap[d] = std::min<uint64_t>(std::max(cap_floor, std::min(want[d], lo)), 0xffffffffull - 64);
+            level_cap = std::max(level_cap, lcap[d]);
+            level[d] = (uint32_t*)(soln + loff);
+            loff += 4ull * (d + 1) * lcap[d];
+        }
+        return true;
     }
     std::vector<uint64_t> counts;
     std::vector<uint64_t> single_counts;
@@ -835,14 +888,13 @@ struct BatchRun {
         FM_CUDA(launch_sched_init(cv.sched, b->maxq, (unsigned long long)nq * base.chunks_per_query * 32, 0,
                                   60000ull * 1000000ull, s));
         BatchParams p = base;
-        p.pstride = b->level_cap;
-        p.ocap = b->level_cap;
         p.ctl = cv.ctl;
         BatchPersistArgs a;
         std::memset(&a, 0, sizeof(a));
         a.sched = cv.sched;
         for (uint32_t d = 0; d < (uint32_t)kMaxQ; d++) {
             a.levels[d] = b->level[d];
+            a.caps[d] = b->lcap[d];
             a.kmax[d] = b->kmax[d];
         }
         a.rings = cv.defs;
@@ -881,6 +933,8 @@ struct BatchRun {
         FM_CUDA(cudaStreamSynchronize(s));
         b->launches += 2;   // the schedule initialisation and the persistent kernel
         const SchedState& h = *cv.h_sched;
+        for (uint32_t d = 0; d < (uint32_t)kMaxQ; d++) b->vol[d] = 0;
+        for (uint32_t d = 1; d + 1 < b->maxq; d++) b->vol[d + 1] = h.lv[d].produced;
         if (h.error & kSchedErrWait) {
             set_error("a bounded wait of the persistent batch kernel ran out (a grid barrier or a list stage)");
             return FM_ERR_DEVICE;
@@ -907,9 +961,9 @@ struct BatchRun {
         p.depth = d;
         p.kmax = b->kmax[d];
         p.pin = d == 1 ? nullptr : b->level[d];
-        p.pstride = b->level_cap;
+        p.pstride = d >= 2 ? b->lcap[d] : 0;
         p.pout = (d + 1 < b->maxq) ? b->level[d + 1] : nullptr;
-        p.ocap = b->level_cap;
+        p.ocap = (d + 1 < b->maxq) ? b->lcap[d + 1] : 0;
         p.def_in = def_list(d, 0);
         p.def_out = def_list(d, 1);
         p.def_cap = cv.def_cap;
@@ -982,6 +1036,7 @@ struct BatchRun {
                     set_error("one 32-parent chunk needs more rows than a level buffer holds; raise SOLN_PREALLOC");
                     return FM_ERR_POOL;
                 }
+                b->vol[d + 1] += c.produced;
                 if (c.produced) FM_TRY(drain(d + 1, c.produced, 0, 0, def_list(d + 1, 0), def_list(d + 1, 1)));
             }
             std::swap(def_a, def_b);
@@ -1018,6 +1073,8 @@ struct BatchRun {
         LaunchCtl snap[kMaxQ];
         std::memcpy(snap, cv.h_ctl, b->maxq * sizeof(LaunchCtl));
         uint64_t n_parents[kMaxQ] = {};
+        for (uint32_t d = 0; d < (uint32_t)kMaxQ; d++) b->vol[d] = 0;
+        for (uint32_t d = 1; d + 1 < b->maxq; d++) b->vol[d + 1] = snap[d].produced;
         for (uint32_t d = 1; d < b->maxq; d++) {
             if (snap[d].error) {
                 set_error((snap[d].error & 2u) ? "a list stage's bounded wait ran out" : "deferred-chunk list overflow");
@@ -1280,6 +1337,7 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
         stats->level_rows = b->level_cap;
         stats->persistent = b->persistent ? 1 : 0;
         stats->graph = (b->replay && b->graph_ok) ? 1 : 0;
+        stats->weighted_levels = b->weighted ? 1 : 0;
         for (uint32_t i = 0; i < b->n; i++) stats->embeddings += b->counts[i];
     }
     if (truncated) {
@@ -1406,18 +1464,33 @@ fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
         bool persistent;
         uint32_t shift, quarters, bank;
     };
+    // bank kWeighted: level buffers sized from the previous run's per-depth volumes
+    constexpr uint32_t kWeighted = 99;
     std::vector<Cand> cands = {{false, 0, 4, 0}, {true, 0, 4, 0}, {false, 1, 4, 0}, {false, 0, 2, 0},
-                               {false, 0, 4, 4}, {false, 0, 4, 8}};
+                               {false, 0, 4, 4}, {false, 0, 4, kWeighted}};
+    uint64_t vol0[kMaxQ];
+    std::memcpy(vol0, b->vol, sizeof(vol0));
+    bool have_vol = false;
+    for (uint32_t d = 2; d < b->maxq; d++) have_vol = have_vol || vol0[d] > 0;
     if (!b->replay) cands.erase(cands.begin() + 1);   // a server's batches use level launches
     double best_ms = -1;
     Cand best_c = {b->persistent, b->piece_shift, b->sm_fraction, b->bank_shift};
     for (const Cand& c : cands) {
-        if (c.bank && (b->cap_full >> c.bank) < b->cap_floor) continue;
+        if (c.bank == kWeighted) {
+            if (!have_vol) continue;
+        } else if (c.bank && (b->cap_full >> c.bank) < b->cap_floor) {
+            continue;
+        }
         b->persistent = c.persistent;
         b->piece_shift = c.shift;
         b->sm_fraction = c.quarters;
         b->bank_shift = c.bank;
-        b->layout_levels(b->cap_full >> c.bank);
+        if (c.bank == kWeighted) {
+            std::memcpy(b->vol, vol0, sizeof(vol0));
+            if (!b->layout_weighted()) continue;
+        } else {
+            b->layout_levels(b->cap_full >> c.bank);
+        }
         b->drop_graphs();
         fm_batch_stats st;
         fm_status s = fm_batch_run(b, nullptr, &st);
@@ -1432,7 +1505,12 @@ fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
     b->piece_shift = bs;
     b->sm_fraction = bq;
     b->bank_shift = bb;
-    b->layout_levels(b->cap_full >> bb);
+    if (bb == kWeighted) {
+        std::memcpy(b->vol, vol0, sizeof(vol0));
+        if (!b->layout_weighted()) b->layout_levels(b->cap_full);
+    } else {
+        b->layout_levels(b->cap_full >> bb);
+    }
     b->drop_graphs();
     if (best) {
         std::memset(best, 0, sizeof(*best));
@@ -1442,6 +1520,7 @@ fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
         best->level_rows = b->level_cap;
         best->persistent = b->persistent ? 1 : 0;
         best->graph = b->graph_ok ? 1 : 0;
+        best->weighted_levels = b->weighted ? 1 : 0;
     }
     return FM_OK;
 }

@@ -269,6 +269,8 @@ typedef struct fm_batch_stats {
     uint64_t level_rows;        /* tuned: rows per level buffer (the bank size) */
     int32_t persistent;         /* 1: one cooperative launch per run (FM_ENGINE_PERSISTENT) */
     int32_t graph;              /* 1: the run is a captured CUDA graph replay */
+    int32_t weighted_levels;    /* 1: level buffers sized from the previous run's per-depth volumes */
+    int32_t reserved;
 } fm_batch_stats;
 
 fm_status fm_batch_create(fm_context* ctx, const fm_graph* g, const fm_query* const* queries, uint32_t n,

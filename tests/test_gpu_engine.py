@@ -93,8 +93,8 @@ def test_persistent_wait_that_runs_out_returns_an_error_and_the_context_survives
                      bank_rows=32)
     g = fm.Graph.from_edges(ctx, G.V, 3, src, dst, lab)
     q = fm.Query.from_text(texts[0])
-    r = fm.match(ctx, g, q, mode=fm.MODE_COUNT, wait_limit_ms=200, test_stall_barrier=True,
-                 allow_device_error=True)
+    r = fm.match(ctx, g, q, mode=fm.MODE_COUNT, engine=fm.ENGINE_PERSISTENT, wait_limit_ms=200,
+                 test_stall_barrier=True, allow_device_error=True)
     assert r.status == fm.FM_ERR_DEVICE and r.engine == fm.ENGINE_PERSISTENT
     assert b"wait" in fm.lib().fm_last_error()
     assert r.max_wait_ns >= 150_000_000
