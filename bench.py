@@ -81,7 +81,7 @@ def run_ncu_step(args):
     """One step of the workload with small knobs, for ncu captures (prints the
     total count; every count is checked against the recorded one).  With
     --workload ingest: the device parse and graph build of a 2^20-vertex,
-    8M-edge R-MAT graph as .g text (about 170 MB)."""
+    8M-edge R-MAT graph as .g text (about 311 MB)."""
     import forkmatch_gb300 as fm
     if args.workload == "ingest":
         from forkmatch_gb300 import synth as S
