@@ -3,7 +3,7 @@ launches replayed as a CUDA graph) beside the plain form (one query per
 launch sequence), on the batched workload, with full uint32 embedding tables.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-  python bench.py --workload plain_at_scale|serving|skew|ingest
+  python bench.py --workload plain_at_scale|plain_small|serving|skew|ingest
 
 Workload (forkmatch_gb300.workloads, default "batched"): R-MAT(0.57, 0.19,
 0.19, 0.05) with 2^22 vertices and 64M distinct undirected edges (128M
@@ -58,7 +58,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched",
-                    choices=["batched", "plain_at_scale", "serving", "skew", "ingest"])
+                    choices=["batched", "plain_at_scale", "plain_small", "serving", "skew", "ingest"])
     ap.add_argument("--ncu-step", action="store_true",
                     help="run one untimed step with small knobs (SOLN 2 GiB, OUTPUT 4.5 GiB) for ncu captures")
     ap.add_argument("--queries", default="all", help="with --ncu-step: comma-separated query indices")
@@ -968,6 +968,52 @@ def run_skew(args, rank, world, local):
     return 0
 
 
+def run_plain_small(args, rank, world, local):
+    """The small plain configuration: Erdos-Renyi 1000 vertices / 2000 edges
+    with 87 edge labels (the er1000_l87 graph of tests/golden/match_cases.json)
+    and its 22 queries, one fm_match at a time, beside the per-query "Kernel
+    Time" the reference's own GPU build printed for the same queries on a
+    GB300 (tests/golden/ref_matches.json).  Device time per query: the median
+    over the timed steps (CUDA events inside the library)."""
+    import torch
+    import forkmatch_gb300 as fm
+    from tests.helpers import load_golden, make_graph
+    torch.cuda.set_device(local)
+    case = [c for c in load_golden("match_cases.json") if c["graph"] == "er1000_l87"][0]
+    ref = {e["query"]: e for g in load_golden("ref_matches.json")["graphs"] if g["graph"] == "er1000_l87"
+           for e in g["cases"]}
+    ctx = fm.Context(prealloc_bytes=2 * GB, soln_prealloc_bytes=512 << 20, output_prealloc_bytes=512 << 20,
+                     device=local)
+    g = fm.Graph.from_text(ctx, make_graph(case["params"]).to_g_text())
+    rows = []
+    for e in case["cases"]:
+        q = fm.Query.from_text(e["text"].encode())
+        for _ in range(args.warmup):
+            fm.match(ctx, g, q, mode=fm.MODE_TABLE)
+        ms = []
+        for _ in range(args.steps):
+            r = fm.match(ctx, g, q, mode=fm.MODE_TABLE)
+            ms.append(r.device_ms)
+            assert r.count == e["count"]
+        rr = ref.get(e["query"], {})
+        rows.append({"query": e["query"], "count": e["count"], "device_ms": float(np.median(ms)),
+                     "reference_kernel_ms": 1000 * rr["kernel_s"] if rr.get("kernel_s") else None,
+                     "reference_count": rr.get("count")})
+    ours = sum(r["device_ms"] for r in rows)
+    theirs = sum(r["reference_kernel_ms"] for r in rows if r["reference_kernel_ms"])
+    n_ref = sum(1 for r in rows if r["reference_kernel_ms"])
+    line = {"metric": "matching time per query", "value": ours / len(rows), "unit": "ms", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "data": "synthetic (seeded)",
+            "config": {"workload": "plain_small", "graph": "Erdos-Renyi 1000 vertices, 2000 edges, 87 edge labels",
+                       "queries": len(rows)},
+            "reference_sm103a_kernel_ms_per_query": theirs / n_ref if n_ref else None,
+            "queries": rows}
+    print(json.dumps(line), flush=True)
+    g.close()
+    ctx.close()
+    return 0
+
+
 def run_ingest(args, rank, world, local):
     """Ingest of the batched workload's graph as .g text (over 2 GiB): the
     text parsed on the device (fm_graph_load_file), parsed on the host into
@@ -1095,6 +1141,8 @@ def main():
         return run_batched(args, rank, world, local)
     if args.workload == "plain_at_scale":
         return run_ours(args, rank, world, local)
+    if args.workload == "plain_small":
+        return run_plain_small(args, rank, world, local)
     if args.workload == "serving":
         return run_serving(args, rank, world, local)
     if args.workload == "skew":
