@@ -88,7 +88,8 @@ class Result(ctypes.Structure):
                 ("rows_copied", ctypes.c_uint64), ("truncated", ctypes.c_int32), ("q", ctypes.c_uint32),
                 ("device_ms", ctypes.c_double), ("launches", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64),
                 ("d2h_bytes", ctypes.c_uint64), ("level", LevelStats * MAXQ), ("engine", ctypes.c_int32),
-                ("passes", ctypes.c_uint32), ("max_wait_ns", ctypes.c_uint64)]
+                ("passes", ctypes.c_uint32), ("max_wait_ns", ctypes.c_uint64), ("pre_counted", ctypes.c_int32),
+                ("reserved", ctypes.c_uint32)]
 
 
 class BatchStats(ctypes.Structure):

@@ -34,6 +34,8 @@ struct BatchPlan {                    // per query, in device memory
     uint64_t root_off;                // roots: heads[root_off .. root_off + n_roots)
     uint32_t n_roots;
     uint32_t count_only;              // no table for this query (count rule allowed)
+    uint32_t pre_ok;                  // last depth has one back edge: when counting, depth q-2 counts
+                                      // each survivor's extensions and depth q-1 is never reached
 };
 
 struct BatchParams {
@@ -128,7 +130,7 @@ struct BMem {
     uint32_t* k_s;      // [32] requirements of the parent's query at this depth
     uint32_t* qid_s;    // [32]
     uint32_t* pidx_s;   // [32] parent index in the level (root vertex at depth 1)
-    uint32_t* fin_s;    // [32] 1 when the parent's query ends at depth d+1
+    uint32_t* fin_s;    // [32] 1: the parent's query ends at this depth; 2: it is pre-counted here
     uint32_t* stp;      // [kBStage] staged parent index
     uint32_t* stx;      // [kBStage] staged vertex
     uint32_t* stq;      // [kBStage] staged query id
@@ -222,7 +224,8 @@ template <bool ROOTS>
 __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem& m, uint32_t chunk, uint32_t lane,
                                                 uint32_t d, unsigned long long n_parents, bool& valid,
                                                 uint32_t& k_out, unsigned long long& words, uint32_t sw,
-                                                uint32_t& phase, bool& stage_ok, unsigned long long& rule_cnt) {
+                                                uint32_t& phase, bool& stage_ok, unsigned long long& rule_cnt,
+                                                uint32_t& cont_total) {
     uint32_t qid, pidx;
     if (ROOTS) {
         qid = chunk / P.chunks_per_query;
@@ -243,7 +246,9 @@ __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem
     if (valid) {
         const BatchPlan& pl = P.plans[qid];
         k = pl.nreq[d];
+        // bit 0: the query ends at this depth; bit 1: it is counted here (pre-count)
         fin = (pl.q == d + 1) ? 1u : 0u;
+        if (pl.q == d + 2 && pl.pre_ok && (!P.table_mode || pl.count_only)) fin = 2u;
         const uint32_t rb = pl.req_begin[d];
         uint32_t best = 0xffffffffu;
         for (uint32_t i = 0; i < k; i++) {
@@ -260,17 +265,14 @@ __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem
         }
         n = best;
         if (k > 2) drv = dev::order_lists(m.segs_s, lane, k, drv);
-        if (fin && k == 1 && (!P.table_mode || pl.count_only)) {
+        if (fin == 1u && k == 1 && (!P.table_mode || pl.count_only)) {
             // Count rule (the query's count only): every entry of the single
             // list extends the parent except the parent's own vertices, so the
             // extensions are counted, not enumerated.  The caller adds the
             // count once, when the main pass keeps the chunk (a chunk can be
             // loaded again after a deferral or for each heavy piece).
             const uint4 sg = m.segs_s[lane];
-            unsigned long long c = sg.x;
-            for (uint32_t a = 0; a < d; a++)
-                c -= seg_has(sg, m.rows_s[a * 32 + lane], 1, P.nbr, P.bm, P.bm_words) ? 1u : 0u;
-            rule_cnt = c;
+            rule_cnt = sg.x - dev::count_members(sg, m.rows_s, lane, d, 0u, false, P.nbr, P.bm, P.bm_words);
             n = 0;
         }
     }
@@ -289,6 +291,9 @@ __device__ __forceinline__ uint32_t bload_chunk(const BatchParams& P, const BMem
     m.qid_s[lane] = qid;
     m.pidx_s[lane] = pidx;
     m.fin_s[lane] = fin;
+    // candidate slots of the parents whose query goes on past this depth: the
+    // only ones whose survivors can take rows of the next level
+    cont_total = __reduce_add_sync(kFull, fin == 0u ? n : 0u);
     __syncwarp();
     return __shfl_sync(kFull, incl, 31);
 }
@@ -339,6 +344,28 @@ __device__ __forceinline__ void bfinal(const BatchParams& P, const BMem& m, bool
     }
 }
 
+// A survivor counted by pre-count (its query's last depth has one back edge):
+// its extensions are the entries of that list minus the row's vertices (the
+// parent's and x) found in it.  Lanes of the same query share one atomic.
+__device__ __forceinline__ void bprecount(const BatchParams& P, const BMem& m, bool pre, uint32_t j, uint32_t x,
+                                          uint32_t lane, uint32_t d) {
+    if (!__ballot_sync(kFull, pre)) return;
+    uint32_t c = 0, qid = 0xffffffffu;
+    if (pre) {
+        qid = m.qid_s[j];
+        const BatchPlan& pl = P.plans[qid];
+        const uint32_t rb = pl.req_begin[d + 1];
+        const uint32_t anc = pl.req_anc[rb];
+        const uint4 sg = ldg4(P.seg + (uint64_t)pl.req_label[rb] * P.V + (anc == d ? x : m.rows_s[anc * 32 + j]));
+        c = sg.x - dev::count_members(sg, m.rows_s, j, d, x, true, P.nbr, P.bm, P.bm_words);
+    }
+    const unsigned grp = __match_any_sync(kFull, qid);
+    const unsigned lo = __reduce_add_sync(grp, c & 0xffffu);
+    const unsigned hi = __reduce_add_sync(grp, c >> 16);
+    if (pre && (int)lane == __ffs(grp) - 1 && (lo | hi))
+        atomicAdd(&P.qpos[qid], ((unsigned long long)hi << 16) + lo);
+}
+
 template <bool ROOTS>
 __device__ __forceinline__ void bprocess(const BatchParams& P, const BMem& m, uint32_t chunk, uint32_t begin,
                                          uint32_t end, uint32_t lane, uint32_t d, uint32_t& nst) {
@@ -360,9 +387,10 @@ __device__ __forceinline__ void bprocess(const BatchParams& P, const BMem& m, ui
             }
             for (uint32_t c = 0; c < d && ok; c++) ok = m.rows_s[c * 32 + j] != x;
         }
-        const bool fin = ok && m.fin_s[j];
-        bfinal(P, m, fin, j, x, lane, d);
-        const bool stage = ok && !fin;
+        const uint32_t fs = ok ? m.fin_s[j] : 0u;
+        bfinal(P, m, fs == 1u, j, x, lane, d);
+        bprecount(P, m, fs == 2u, j, x, lane, d);
+        const bool stage = ok && fs == 0u;
         const unsigned b = __ballot_sync(kFull, stage);
         if (stage) {
             const uint32_t q0 = nst + __popc(b & ((1u << lane) - 1u));
@@ -424,20 +452,22 @@ __device__ __forceinline__ void bexpand_main(const BatchParams& P, unsigned char
             bool valid, stage_ok;
             uint32_t k;
             unsigned long long w, rule_cnt;
+            uint32_t cont;
             const uint32_t total = bload_chunk<ROOTS>(P, m, chunk, lane, d, T.n_parents, valid, k, w, sw, phase,
-                                                      stage_ok, rule_cnt);
+                                                      stage_ok, rule_cnt, cont);
             last_chunk = chunk;
             if (!stage_ok) {
                 done = true;
                 break;
             }
-            // only survivors of queries that go on use the next level's buffer;
-            // the upper bound of the whole chunk is reserved (over-reserving is safe)
-            if (total && P.pout) {
+            // only survivors of queries that go on use the next level's buffer:
+            // the upper bound of their candidates is reserved (survivors that end
+            // their query here, or are pre-counted, take no row)
+            if (cont && P.pout) {
                 int ok = 1;
-                if (lane == 0 && total > credit) {
+                if (lane == 0 && cont > credit) {
                     const unsigned long long need =
-                        max((unsigned long long)total, (unsigned long long)T.credit_block);
+                        max((unsigned long long)cont, (unsigned long long)T.credit_block);
                     const unsigned long long old = atomicAdd(&P.ctl->budget, need);
                     if (old + need > P.ocap) {
                         ok = 0;
@@ -447,7 +477,7 @@ __device__ __forceinline__ void bexpand_main(const BatchParams& P, unsigned char
                         credit += need;
                     }
                 }
-                if (lane == 0 && ok) credit -= total;
+                if (lane == 0 && ok) credit -= cont;
                 ok = __shfl_sync(kFull, ok, 0);
                 if (!ok) {
                     done = true;
@@ -537,7 +567,8 @@ __device__ __forceinline__ void bexpand_heavy(const BatchParams& P, unsigned cha
         bool valid, stage_ok;
         uint32_t k;
         unsigned long long w, rule_cnt;   // counted by the main pass
-        bload_chunk<ROOTS>(P, m, e.chunk, lane, d, T.n_parents, valid, k, w, sw, phase, stage_ok, rule_cnt);
+        uint32_t cont;
+        bload_chunk<ROOTS>(P, m, e.chunk, lane, d, T.n_parents, valid, k, w, sw, phase, stage_ok, rule_cnt, cont);
         last_chunk = e.chunk;
         if (!stage_ok) break;
         bprocess<ROOTS>(P, m, e.chunk, begin, end, lane, d, nst);
@@ -834,6 +865,7 @@ void build_plan(const Plan& pl, const DeviceGraph& g, BatchPlan& bp, bool& impos
         const uint32_t col = q - 1 - ref_depth[order[d]];
         bp.col_depth[col] = (uint8_t)d;
     }
+    bp.pre_ok = (q >= 3 && nreq[q - 1] == 1 && pre_count_knob()) ? 1u : 0u;
     // roots: the vertices with an e-line of a depth-1 label (the shortest list)
     bool first = true;
     for (uint32_t i = 0; i < nreq[1] && !impossible; i++) {

@@ -10,6 +10,14 @@ constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ uint4 ldg4(const uint4* p) { return __ldg(p); }
 
+// Sum of one u32 per lane over the full warp, exact (two 16-bit halves, each
+// sum below 2^21).
+__device__ __forceinline__ unsigned long long warp_sum_u32(uint32_t v) {
+    const unsigned lo = __reduce_add_sync(kFull, v & 0xffffu);
+    const unsigned hi = __reduce_add_sync(kFull, v >> 16);
+    return ((unsigned long long)hi << 16) + lo;
+}
+
 // Element t of a (label, vertex) list given its segment record.
 __device__ __forceinline__ uint32_t seg_at(const uint4& s, uint32_t t, const uint32_t* __restrict__ nbr) {
     if (s.x <= 3) return t == 0 ? s.y : (t == 1 ? s.z : s.w);
@@ -48,6 +56,62 @@ __device__ __forceinline__ bool seg_has(const uint4& s, uint32_t x, uint32_t nee
     const uint32_t* a = nbr + (uint64_t)s.y * 4;
     const uint32_t pos = lower_bound_g(a, s.x, x) + need - 1;
     return pos < s.x && __ldg(a + pos) == x;
+}
+
+// How many of the row's vertices (column-major rows_s[c*32 + j], c < n_row)
+// and, with `extra`, the value x, are in the list of record s.  Graphs
+// without duplicate e-lines only (a value is in a list at most once); the
+// values are distinct (an injective row plus a new vertex).  Used by the
+// count rule, where every one of these membership tests is needed: inline
+// lists compare in registers, bitmap lists take one independent load per
+// value, and long lists are searched for four values in lockstep
+// (branch-free search for the last entry <= value: every step issues its
+// four loads together, so the searches overlap instead of running one after
+// another).
+__device__ __forceinline__ uint32_t count_members(const uint4& s, const uint32_t* rows_s, uint32_t j, uint32_t n_row,
+                                                  uint32_t x, bool extra, const uint32_t* __restrict__ nbr,
+                                                  const uint32_t* __restrict__ bm, uint32_t bm_words) {
+    const uint32_t n = n_row + (extra ? 1u : 0u);
+    uint32_t found = 0;
+    if (s.x == 0) return 0;
+    if (s.x <= 3) {
+        for (uint32_t i = 0; i < n; i++) {
+            const uint32_t v = i < n_row ? rows_s[i * 32 + j] : x;
+            found += (s.y == v) + (s.x > 1 && s.z == v) + (s.x > 2 && s.w == v);
+        }
+        return found;
+    }
+    if (s.z & kBitmapMark) {
+        const uint32_t* b = bm + (uint64_t)(s.z & ~kBitmapMark) * bm_words;
+        for (uint32_t i = 0; i < n; i++) {
+            const uint32_t v = i < n_row ? rows_s[i * 32 + j] : x;
+            found += v <= s.w ? (__ldg(b + (v >> 5)) >> (v & 31)) & 1u : 0u;
+        }
+        return found;
+    }
+    const uint32_t* a = nbr + (uint64_t)s.y * 4;
+    for (uint32_t g = 0; g < n; g += 4) {
+        uint32_t key[4], base[4];
+        bool act[4];
+#pragma unroll
+        for (uint32_t u = 0; u < 4; u++) {
+            const uint32_t i = g + u;
+            key[u] = i < n_row ? rows_s[i * 32 + j] : x;
+            act[u] = i < n && key[u] >= s.z && key[u] <= s.w;
+            base[u] = 0;
+        }
+        uint32_t len = s.x;
+        while (len > 1) {
+            const uint32_t half = len >> 1;
+#pragma unroll
+            for (uint32_t u = 0; u < 4; u++)
+                if (act[u] && __ldg(a + base[u] + half) <= key[u]) base[u] += half;
+            len -= half;
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < 4; u++) found += (act[u] && __ldg(a + base[u]) == key[u]) ? 1u : 0u;
+    }
+    return found;
 }
 
 // ------------------------------------------------- staged membership lists

@@ -79,6 +79,11 @@ uint32_t fm::stage_words_knob() {
     return w;
 }
 
+bool fm::pre_count_knob() {
+    static const bool on = env_u64("FM_PRE_COUNT", 1) != 0;
+    return on;
+}
+
 namespace {
 
 // [0, 4 KiB) control blocks, [4 KiB, 8 KiB) match totals and the persistent
@@ -479,6 +484,12 @@ struct MatchRun {
     size_t prof_used = 0;
     int block = 256;
     uint64_t work_limit = 0;         // partial matches produced, checked between launches
+    // count mode with one back edge at the last depth: depth q-2 counts its
+    // survivors' extensions (ExpandParams::pre_count) and depth q-1 is never
+    // launched
+    bool pre = false;
+
+    uint32_t last_depth() const { return plan->q - 1 - (pre ? 1u : 0u); }
 
     bool over_limit() const {
         if (!work_limit) return false;
@@ -488,7 +499,24 @@ struct MatchRun {
     }
 
     int mode_of(uint32_t d) const {
-        return (d == plan->q - 1) ? (table ? kModeLastTable : kModeLastCount) : kModeMid;
+        return (d == last_depth()) ? (table ? kModeLastTable : kModeLastCount) : kModeMid;
+    }
+
+    // Pre-count: the last depth's work counters, which the counting level
+    // added to the last depth's control block, and the counting level's
+    // survivors (its "produced" rows, never stored).
+    fm_status finish_pre() {
+        if (!pre) return FM_OK;
+        const uint32_t q = plan->q;
+        FM_CUDA(cudaMemcpyAsync(ctx->h_ctl + q - 1, ctx->ctl + q - 1, sizeof(LaunchCtl), cudaMemcpyDeviceToHost, s));
+        FM_CUDA(cudaStreamSynchronize(s));
+        const LaunchCtl& c = ctx->h_ctl[q - 1];
+        fm_level_stats& ls = res->level[q - 1];
+        ls.parents = c.parents;
+        ls.lookups = c.lookups;
+        ls.list_words = c.list_words;
+        res->level[q - 2].produced = c.parents;
+        return FM_OK;
     }
     uint32_t* def_list(uint32_t d, int which) const {
         return ctx->defs + (size_t)(2 * d + which) * ctx->def_cap;
@@ -522,8 +550,10 @@ struct MatchRun {
     // deeper level still has to read.
     fm_status run(uint64_t n_roots) {
         const uint32_t q = plan->q;
+        const uint32_t last = last_depth();
         cudaEvent_t ev[kMaxQ][2] = {};
-        for (uint32_t d = 1; d < q; d++) {
+        if (pre) FM_CUDA(cudaMemsetAsync(ctx->ctl + q - 1, 0, sizeof(LaunchCtl), s));
+        for (uint32_t d = 1; d <= last; d++) {
             const int mode = mode_of(d);
             const bool roots = d == 1;
             const size_t smem = expand_smem_bytes(d, nreq_depth[d], block / 32,
@@ -558,7 +588,7 @@ struct MatchRun {
         FM_CUDA(cudaMemcpyAsync(ctx->h_ctl, ctx->ctl, q * sizeof(LaunchCtl), cudaMemcpyDeviceToHost, s));
         FM_CUDA(cudaStreamSynchronize(s));
         uint64_t n_parents[kMaxQ] = {};
-        for (uint32_t d = 1; d < q; d++) {
+        for (uint32_t d = 1; d <= last; d++) {
             const LaunchCtl& c = ctx->h_ctl[d];
             n_parents[d] = d == 1 ? n_roots : ctx->h_ctl[d - 1].produced;
             add_stats(d, c);
@@ -575,7 +605,7 @@ struct MatchRun {
         if (over_limit()) return FM_ERR_LIMIT;
         LaunchCtl snap[kMaxQ];
         std::memcpy(snap, ctx->h_ctl, q * sizeof(LaunchCtl));
-        for (uint32_t d = q - 1; d >= 1; d--) {
+        for (uint32_t d = last; d >= 1; d--) {
             if (mode_of(d) != kModeMid) continue;   // the last level never defers
             const LaunchCtl& c = snap[d];
             const uint64_t items = (n_parents[d] + 31) / 32;
@@ -586,7 +616,7 @@ struct MatchRun {
             fm_status st = drain_level(d, n_parents[d], d == 1, c.ndef, claimed, def_list(d, 1), def_list(d, 0));
             if (st != FM_OK) return st;
         }
-        return FM_OK;
+        return finish_pre();
     }
 
     // Persistent engine: one cooperative launch runs every pass; the device
@@ -648,7 +678,7 @@ struct MatchRun {
             return FM_ERR_POOL;
         }
         if (h.error & kSchedErrLimit) return FM_ERR_LIMIT;
-        return FM_OK;
+        return finish_pre();
     }
 
     // Host-driven depth-first loop for one level (used when a level's buffer
@@ -843,8 +873,12 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         }
         out->count = n;
     } else if (!impossible && re > rb) {
+        // pre-count: the last depth is counted from depth q-2, so it needs no
+        // level buffer (graphs with duplicate e-lines enumerate it)
+        run.pre = !table && !g.has_dups && q >= 3 && nreq[q - 1] == 1 && pre_count_knob();
+        const uint32_t stored = q - (run.pre ? 1u : 0u);   // depths with a level buffer: 2 .. stored-1
         uint64_t sum_cols = 0;
-        for (uint32_t d = 2; d < q; d++) sum_cols += d;
+        for (uint32_t d = 2; d < stored; d++) sum_cols += d;
         uint64_t cap = sum_cols ? ctx->soln_bytes / (4ull * sum_cols) : 0;
         const uint64_t bank = ctx->knobs.bank_rows;
         if (sum_cols) {
@@ -866,7 +900,7 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         run.profile = opts.profile != 0;
         uint64_t off = 0;
         for (uint32_t d = 0; d < kMaxQ; d++) run.level[d] = nullptr;
-        for (uint32_t d = 2; d < q; d++) {
+        for (uint32_t d = 2; d < stored; d++) {
             run.level[d] = (uint32_t*)(ctx->soln + off);
             off += 4ull * d * cap;
         }
@@ -901,6 +935,8 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         b.heavy_cap = ctx->heavy_cap;
         b.work_limit = opts.work_limit;
         b.stage_words = stage_words_knob();
+        b.pre_count = run.pre ? 1u : 0u;
+        out->pre_counted = run.pre ? 1 : 0;
         run.work_limit = opts.work_limit;
         fm_status st = FM_ERR_UNSUPPORTED;
         out->engine = FM_ENGINE_LEVELS;

@@ -191,6 +191,13 @@ struct ExpandParams {
     // by TMA (levels with two or more back edges); 0 = lists are searched in
     // global memory
     uint32_t stage_words;
+    // Count mode, the query's last depth has one back edge (no duplicate
+    // e-lines): the counting level is depth q-2, whose survivors are not
+    // stored but counted by their extensions (the single list's length minus
+    // the row's vertices found in it); depth q-1 is never launched.  Its work
+    // counters (parents, lookups, list words) are added to ctl[1] of the
+    // counting level's control block array (the next depth's block).
+    uint32_t pre_count;
 };
 constexpr unsigned int kLimitFlag = 2u;
 
@@ -241,6 +248,9 @@ struct PersistArgs {
 size_t persist_smem_bytes(const DevPlan& plan, const uint32_t* nreq_depth, uint32_t stage_words);
 // Words of the per-warp membership-list stage (FM_STAGE_WORDS, read once).
 uint32_t stage_words_knob();
+// Count the last depth from depth q-2 when it has one back edge (FM_PRE_COUNT,
+// default 1; 0 launches the last depth as its own level).
+bool pre_count_knob();
 int persist_blocks_per_sm(int last_mode, bool dups, size_t smem);
 cudaError_t launch_persist(const ExpandParams& p, const PersistArgs& a, int last_mode, bool dups, int grid,
                            size_t smem, cudaStream_t s);

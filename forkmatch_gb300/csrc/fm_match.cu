@@ -341,6 +341,29 @@ __device__ __forceinline__ uint32_t load_chunk(const ExpandParams& P, const Warp
     return __shfl_sync(kFull, incl, 31);
 }
 
+// Work counters of the last depth under pre-count (lane-private): the
+// survivors stand for that depth's parents, one lookup each, and their
+// lists' lengths for its list words.
+struct PreAcc {
+    unsigned long long parents = 0, words = 0;
+};
+
+// Adds a warp's pre-count work counters to the next depth's control block,
+// so the last depth reports the same work as when it is launched.
+__device__ __forceinline__ void flush_pre(const ExpandParams& P, PreAcc& pre, uint32_t lane) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        pre.parents += __shfl_down_sync(kFull, pre.parents, o);
+        pre.words += __shfl_down_sync(kFull, pre.words, o);
+    }
+    if (lane == 0 && pre.parents) {
+        LaunchCtl* next = P.ctl + 1;
+        atomicAdd(&next->parents, pre.parents);
+        atomicAdd(&next->lookups, pre.parents);
+        atomicAdd(&next->list_words, pre.words);
+    }
+}
+
 // Evaluate slots [begin, end) of the loaded chunk: kSlots slots per lane per
 // round with all their driver loads in flight; survivors go to the stage,
 // which is flushed whenever it cannot take another round.
@@ -348,7 +371,7 @@ template <int MODE, bool ROOTS, bool DUPS>
 __device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpMem& m, uint32_t chunk,
                                               uint32_t begin, uint32_t end, uint32_t lane, uint32_t d, uint32_t k,
                                               const uint8_t* col_depth_s, uint32_t& nst,
-                                              unsigned long long& n_count) {
+                                              unsigned long long& n_count, PreAcc& pre) {
     const uint32_t pbase = chunk * 32;
     for (uint32_t base = begin; base < end; base += 32 * kSlots) {
         uint32_t j[kSlots], t[kSlots], x[kSlots];
@@ -371,6 +394,26 @@ __device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpM
                 ok[u] = slot_check<DUPS>(P, x[u], t[u], j[u], dj, m.segs_s[dj * 32 + j[u]], m.segs_s, m.rows_s, k, d,
                                          m.stage);
             }
+        }
+        if (MODE == kModeLastCount && !DUPS && P.pre_count) {
+            // Pre-count: each survivor's extensions at the last depth (one back
+            // edge: ancestor anc, label lab) are the entries of that list minus
+            // the row's vertices found in it; the survivor is never stored.
+            const uint32_t rb = P.plan.req_begin[d + 1];
+            const uint32_t anc = P.plan.req_anc[rb];
+            const uint4* segl = P.seg + (uint64_t)P.plan.req_label[rb] * P.V;
+#pragma unroll
+            for (uint32_t u = 0; u < kSlots; u++) {
+                uint32_t c = 0;
+                if (ok[u]) {
+                    const uint4 sg = ldg4(segl + (anc == d ? x[u] : m.rows_s[anc * 32 + j[u]]));
+                    c = sg.x - dev::count_members(sg, m.rows_s, j[u], d, x[u], true, P.nbr, P.bm, P.bm_words);
+                    pre.parents += 1;
+                    pre.words += sg.x;
+                }
+                n_count += dev::warp_sum_u32(c);
+            }
+            continue;
         }
         const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
@@ -439,6 +482,7 @@ __device__ __forceinline__ void expand_main(const ExpandParams& P, unsigned char
 
     unsigned long long n_count = 0, n_lookups = 0, n_words = 0, n_parents = 0;
     unsigned long long n_flushed = 0;  // part of n_count already added to tot->count (lane 0)
+    PreAcc pre;
     uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
     unsigned long long credit = 0;   // level budget held by this warp (lane 0)
     uint32_t nst = 0;
@@ -477,7 +521,7 @@ __device__ __forceinline__ void expand_main(const ExpandParams& P, unsigned char
                 done = true;
                 break;
             }
-            if (MODE == kModeLastCount && !DUPS && k == 1) {
+            if (MODE == kModeLastCount && !DUPS && k == 1 && !P.pre_count) {
                 // Count rule: with one requirement every list entry extends the
                 // parent except the parent's own vertices, so each lane counts
                 // its parent's extensions as the list length minus the row's
@@ -485,9 +529,7 @@ __device__ __forceinline__ void expand_main(const ExpandParams& P, unsigned char
                 unsigned long long c = 0;
                 if (valid) {
                     const uint4 sg = m.segs_s[lane];
-                    c = sg.x;
-                    for (uint32_t a = 0; a < d; a++)
-                        c -= seg_has(sg, m.rows_s[a * 32 + lane], 1, P.nbr, P.bm, P.bm_words) ? 1u : 0u;
+                    c = sg.x - dev::count_members(sg, m.rows_s, lane, d, 0u, false, P.nbr, P.bm, P.bm_words);
                     n_lookups += k;
                     n_words += w;
                     n_parents += 1;
@@ -546,7 +588,7 @@ __device__ __forceinline__ void expand_main(const ExpandParams& P, unsigned char
                 pub = __shfl_sync(kFull, pub, 0);
                 if (pub) continue;
             }
-            process_slots<MODE, ROOTS, DUPS>(P, m, chunk, 0, total, lane, d, k, col_depth_s, nst, n_count);
+            process_slots<MODE, ROOTS, DUPS>(P, m, chunk, 0, total, lane, d, k, col_depth_s, nst, n_count, pre);
         }
     }
     if (MODE != kModeLastCount && nst) flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s, last_chunk);
@@ -564,6 +606,7 @@ __device__ __forceinline__ void expand_main(const ExpandParams& P, unsigned char
         }
         if (MODE == kModeLastCount && n_count > n_flushed) atomicAdd(&P.tot->count, n_count - n_flushed);
     }
+    if (MODE == kModeLastCount && !DUPS && P.pre_count) flush_pre(P, pre, lane);
 }
 
 // Heavy pass (after the main pass): every warp claims pieces of the published
@@ -585,6 +628,7 @@ __device__ __forceinline__ void expand_heavy(const ExpandParams& P, unsigned cha
     const WarpMem m = warp_mem(smem_raw, threadIdx.x >> 5, d, k, sw, mbar_s);
     const Tune T = make_tune(P, false);
     unsigned long long n_count = 0, n_flushed = 0;
+    PreAcc pre;
     uint32_t last_chunk = 0xffffffffu;   // chunk whose rows are in m.rows_s
     uint32_t nst = 0;
     for (;;) {
@@ -607,10 +651,11 @@ __device__ __forceinline__ void expand_heavy(const ExpandParams& P, unsigned cha
         load_chunk<ROOTS>(P, m, e.chunk, lane, d, k, rb, T.n_parents, valid, w, phase, stage_ok);
         last_chunk = e.chunk;
         if (!stage_ok) break;
-        process_slots<MODE, ROOTS, DUPS>(P, m, e.chunk, begin, end, lane, d, k, col_depth_s, nst, n_count);
+        process_slots<MODE, ROOTS, DUPS>(P, m, e.chunk, begin, end, lane, d, k, col_depth_s, nst, n_count, pre);
     }
     if (MODE != kModeLastCount && nst) flush_stage<MODE, ROOTS>(P, m, nst, lane, d, col_depth_s, last_chunk);
     if (MODE == kModeLastCount && lane == 0 && n_count > n_flushed) atomicAdd(&P.tot->count, n_count - n_flushed);
+    if (MODE == kModeLastCount && !DUPS && P.pre_count) flush_pre(P, pre, lane);
 }
 
 template <int MODE, bool ROOTS, bool DUPS>
@@ -701,7 +746,7 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_persist(const __grid_constan
                 const unsigned long long n_chunks = (L->n_parents + 31) / 32;
                 P.depth = d;
                 P.pin = d == 1 ? nullptr : A.levels[d];
-                P.pout = d + 1 < q ? A.levels[d + 1] : nullptr;
+                P.pout = d + 1 + P0.pre_count < q ? A.levels[d + 1] : nullptr;
                 P.n_parents = L->n_parents;
                 P.ndef_in = (uint32_t)ring;
                 P.fresh_base = L->fresh;
@@ -718,7 +763,7 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_persist(const __grid_constan
         __syncthreads();
         const unsigned d = cur_s;
         if (d == 0) break;
-        const bool roots = d == 1, last = d + 1 == q;
+        const bool roots = d == 1, last = d + 1 + P0.pre_count == q;
         persist_main<LAST, DUPS>(P, smem_raw, col_depth_s, roots, last, mbar_s, phase);
         if (!dev::grid_barrier(S, first && A.hold_first_barrier && blockIdx.x == 0, &flag_s)) break;
         first = false;

@@ -240,6 +240,10 @@ typedef struct fm_result {
     int32_t engine;             /* fm_engine that ran */
     uint32_t passes;            /* level passes over all depths */
     uint64_t max_wait_ns;       /* persistent engine: longest grid-barrier wait of a block */
+    int32_t pre_counted;        /* count mode, last depth with one back edge: its extensions were
+                                   counted from depth q-2 (its survivors are not stored), so the
+                                   last depth was not launched; level[q-1] still reports its work */
+    uint32_t reserved;
 } fm_result;
 
 fm_status fm_match(fm_context* ctx, const fm_graph* g, const fm_query* q,
