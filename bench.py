@@ -77,6 +77,25 @@ def parse_args():
     return ap.parse_args()
 
 
+def match_alg_bytes(r, qi, count_only):
+    """Algorithmic bytes of one match from its per-level work counters: per
+    depth, 16 B per (vertex, label) record lookup, 4 B per word of the
+    looked-up lists and 8 B per partial match stored in a level buffer; 4q B
+    per table row.  The last depth stores no partial matches (its rows are
+    table rows, or only counted).  A count-only last depth with one back edge
+    is charged its lookups only (the count rule: one record per parent, the
+    parent's vertices tested against it), and the depth before it stores
+    nothing when the match counted from there (pre-count)."""
+    q = qi.q
+    b = 0
+    for d in range(1, q):
+        lv = r.level[d]
+        rule = count_only and d == q - 1 and qi.nreq[d] == 1
+        stored = d < q - 1 and not (r.pre_counted and d == q - 2)
+        b += 16 * lv.lookups + (0 if rule else 4 * lv.list_words) + (8 * lv.produced if stored else 0)
+    return b + (0 if count_only else 4 * q * r.count)
+
+
 def run_ncu_step(args):
     """One step of the workload with small knobs, for ncu captures (prints the
     total count; every count is checked against the recorded one).  With
@@ -114,11 +133,7 @@ def run_ncu_step(args):
         for q, c_only in zip(qs, counted):
             qi = q.info()
             r = fm.match(ctx, g, q, mode=fm.MODE_COUNT if c_only else fm.MODE_TABLE, profile=True)
-            for d in range(1, qi.q):
-                lv = r.level[d]
-                rule = c_only and d == qi.q - 1 and qi.nreq[d] == 1
-                alg += 16 * lv.lookups + (0 if rule else 4 * lv.list_words) + 8 * lv.produced
-            alg += 0 if c_only else 4 * qi.q * r.count
+            alg += match_alg_bytes(r, qi, c_only)
         b = fm.Batch(ctx, g, qs, mode=fm.MODE_TABLE)
         for i, c_only in enumerate(counted):
             if c_only:
@@ -389,11 +404,9 @@ def run_ours(args, rank, world, local):
     n_launch = 0
     for r, qi in zip(prof, qinfo):
         for d in range(1, qi.q):
-            lv = r.level[d]
-            alg_bytes += 16 * lv.lookups + 4 * lv.list_words + 8 * lv.produced
-            kern_ms += lv.kernel_ms
-            n_launch += lv.launches
-        alg_bytes += 4 * qi.q * r.count
+            kern_ms += r.level[d].kernel_ms
+            n_launch += r.level[d].launches
+        alg_bytes += match_alg_bytes(r, qi, False)
     peak, peak_kind = measured_peak_hbm()
     achieved = alg_bytes / (kern_ms / 1000.0) / 1e9 if kern_ms > 0 else None
 
@@ -545,9 +558,11 @@ def batched_config(wl, G, same):
                          "2^22; count-only queries: 4-vertex paths and stars pinned by exact closed forms, "
                          "5-vertex paths by the oracle with the count rule; larger paths, stars and cycles are "
                          "excluded with GPU time estimates (their slots hold walk subgraphs)",
-            "mode": "batched: one persistent cooperative launch for all queries replayed as a CUDA graph, "
-                    "autotuned split granularity, grid and level-buffer size; per-query uint64 counts + uint32 "
-                    "tables (count-only queries: counts). plain: one fm_match per query",
+            "mode": "batched: shared level launches (or one persistent cooperative launch) for all queries, "
+                    "replayed as a CUDA graph; the autotuner picks the queries matched alone inside the run (those "
+                    "whose work fills the GPU by itself: single-query engine, whole level memory), the engine, split "
+                    "granularity, grid and level-buffer size; per-query uint64 counts + uint32 tables (count-only "
+                    "queries: counts). plain: one fm_match per query",
             "graph_matches_recorded_hash": same,
             "l2": "inputs larger than L2: resident graph 5.7 GB vs 129 MB L2; no flush between steps"}
 
@@ -634,19 +649,10 @@ def run_batched(args, rank, world, local):
         plain_rows[i] = rows[np.lexsort(rows.T[::-1])] if len(rows) else rows
 
     # roofline numerator: the algorithmic bytes of every query (same matching
-    # order in both forms), from the plain form's per-level counters.  A
-    # count-only query's last level reads one record per parent and tests the
-    # parent's vertices against it (the count rule), so its list words are not
-    # charged; a table query's rows are.
+    # order in both forms), from the plain form's per-level counters
     prof = []
     plain_step(collect=prof, profile=True)
-    alg_bytes = 0
-    for r, qi, c_only in zip(prof, qinfo, counted):
-        for d in range(1, qi.q):
-            lv = r.level[d]
-            rule = c_only and d == qi.q - 1 and qi.nreq[d] == 1
-            alg_bytes += 16 * lv.lookups + (0 if rule else 4 * lv.list_words) + 8 * lv.produced
-        alg_bytes += 0 if c_only else 4 * qi.q * r.count
+    alg_bytes = sum(match_alg_bytes(r, qi, c_only) for r, qi, c_only in zip(prof, qinfo, counted))
 
     b = fm.Batch(ctx, g, queries, mode=fm.MODE_TABLE)
     for i, c_only in enumerate(counted):
@@ -700,9 +706,16 @@ def run_batched(args, rank, world, local):
     host = fm.PinnedRows(table_words + 1, 1)
     texts = [q["text"].encode() for q in meta]
 
+    # a later batch of the same queries reuses the tuner's choices that are
+    # per query or per engine (the queries matched alone, the engine)
+    solo_idx = b.solo()
+
     def e2e_fresh():
         qs = [fm.Query.from_text(tx) for tx in texts]
         bb = fm.Batch(ctx, g, qs, mode=fm.MODE_TABLE)
+        bb.set_engine(fm.ENGINE_PERSISTENT if st.persistent else fm.ENGINE_LEVELS)
+        for i in solo_idx:
+            bb.set_solo(i)
         for i, c_only in enumerate(counted):
             if c_only:
                 bb.set_query_mode(i, fm.MODE_COUNT)
@@ -766,7 +779,8 @@ def run_batched(args, rank, world, local):
                       "piece_shift": tune.piece_shift, "grid_quarters": tune.grid_quarters,
                       "level_rows": tune.level_rows, "weighted_levels": bool(st.weighted_levels),
                       "persistent": bool(st.persistent), "graph": bool(st.graph),
-                      "batched_queries": st.batched_queries, "single_queries": st.single_queries},
+                      "batched_queries": st.batched_queries, "single_queries": st.single_queries,
+                      "solo_queries": st.solo_queries},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": batched_traffic(alg_bytes / max(1, world)),
                          "kernel": "k_bexpand + k_bexpand_heavy (one batch run; k_bpersist when the tuner picks the persistent engine)",

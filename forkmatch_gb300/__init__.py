@@ -41,7 +41,8 @@ EXPORTS = [
     "fm_match_static", "fm_batch_create", "fm_batch_run", "fm_batch_rows", "fm_batch_copy_rows", "fm_batch_tune",
     "fm_batch_free", "fm_batch_copy_tables", "fm_server_create", "fm_server_submit", "fm_server_poll",
     "fm_server_release", "fm_server_get_stats", "fm_server_destroy", "fm_graph_write_cache", "fm_table_write",
-    "fm_table_to_query_columns", "fm_batch_set_engine", "fm_batch_set_query_mode",
+    "fm_table_to_query_columns", "fm_batch_set_engine", "fm_batch_set_query_mode", "fm_batch_set_solo",
+    "fm_batch_get_solo",
 ]
 
 
@@ -97,7 +98,7 @@ class BatchStats(ctypes.Structure):
                 ("batched_queries", ctypes.c_uint32), ("single_queries", ctypes.c_uint32),
                 ("piece_shift", ctypes.c_uint32), ("grid_quarters", ctypes.c_uint32),
                 ("level_rows", ctypes.c_uint64), ("persistent", ctypes.c_int32), ("graph", ctypes.c_int32),
-                ("weighted_levels", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("weighted_levels", ctypes.c_int32), ("solo_queries", ctypes.c_int32)]
 
 
 class ServerOpts(ctypes.Structure):
@@ -157,6 +158,8 @@ def lib():
         L.fm_batch_run.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(BatchStats)]
         L.fm_batch_set_engine.argtypes = [vp, i32]
         L.fm_batch_set_query_mode.argtypes = [vp, u32, i32]
+        L.fm_batch_set_solo.argtypes = [vp, u32, i32]
+        L.fm_batch_get_solo.argtypes = [vp, u32, ctypes.POINTER(i32)]
         L.fm_batch_rows.argtypes = [vp, u32, ctypes.POINTER(vp), ctypes.POINTER(u64)]
         L.fm_batch_copy_rows.argtypes = [vp, u32, vp, u64, ctypes.POINTER(u64)]
         L.fm_batch_copy_tables.argtypes = [vp, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]
@@ -412,6 +415,20 @@ class Batch:
 
     def set_engine(self, engine):
         _check(lib().fm_batch_set_engine(self._h, int(engine)), "fm_batch_set_engine")
+
+    def set_solo(self, i, solo=True):
+        """Match query i alone inside later runs (or back in the shared launches)."""
+        _check(lib().fm_batch_set_solo(self._h, int(i), 1 if solo else 0), "fm_batch_set_solo")
+
+    def solo(self):
+        """Indices of the queries matched alone (chosen by tune() or set_solo)."""
+        out = []
+        for i in range(len(self.queries)):
+            v = ctypes.c_int32()
+            _check(lib().fm_batch_get_solo(self._h, i, ctypes.byref(v)), "fm_batch_get_solo")
+            if v.value:
+                out.append(i)
+        return out
 
     def tune(self):
         st = BatchStats()

@@ -90,6 +90,7 @@ using dev::slot_locate;
 
 constexpr int kBWarps = 8;
 constexpr uint32_t kBStage = 128;
+constexpr uint32_t kBSlots = 2;            // candidate slots per lane per round
 constexpr uint32_t kHeavyMaxPieces = 65536;
 
 struct BTune {
@@ -366,40 +367,52 @@ __device__ __forceinline__ void bprecount(const BatchParams& P, const BMem& m, b
         atomicAdd(&P.qpos[qid], ((unsigned long long)hi << 16) + lo);
 }
 
+// Evaluate slots [begin, end) of the loaded chunk, kBSlots per lane per round
+// with every driver load of the round issued before any check (as in the
+// single-query kernel); each slot's survivor is then counted or written
+// (its query ends here), pre-counted, or staged for the next level.
 template <bool ROOTS>
 __device__ __forceinline__ void bprocess(const BatchParams& P, const BMem& m, uint32_t chunk, uint32_t begin,
                                          uint32_t end, uint32_t lane, uint32_t d, uint32_t& nst) {
-    for (uint32_t base = begin; base < end; base += 32) {
-        const uint32_t s = base + lane;
-        bool ok = false;
-        uint32_t j = 0, x = 0;
-        if (s < end) {
-            uint32_t t;
-            slot_locate(s, m.excl_s, j, t);
-            const uint32_t dj = m.drv_s[j];
-            const uint4 ds = m.segs_s[dj * 32 + j];
-            x = seg_at(ds, t, P.nbr);
-            ok = true;
-            const uint32_t k = m.k_s[j];
-            for (uint32_t i = 0; i < k && ok; i++) {
-                if (i == dj) continue;
-                ok = dev::seg_has_st(m.segs_s[i * 32 + j], x, 1, P.nbr, P.bm, P.bm_words, m.stage);
+    for (uint32_t base = begin; base < end; base += 32 * kBSlots) {
+        uint32_t j[kBSlots], t[kBSlots], x[kBSlots];
+        bool ok[kBSlots];
+#pragma unroll
+        for (uint32_t u = 0; u < kBSlots; u++) {
+            const uint32_t s = base + 32 * u + lane;
+            j[u] = t[u] = x[u] = 0;
+            ok[u] = s < end;
+            if (ok[u]) {
+                slot_locate(s, m.excl_s, j[u], t[u]);
+                x[u] = seg_at(m.segs_s[m.drv_s[j[u]] * 32 + j[u]], t[u], P.nbr);
             }
-            for (uint32_t c = 0; c < d && ok; c++) ok = m.rows_s[c * 32 + j] != x;
         }
-        const uint32_t fs = ok ? m.fin_s[j] : 0u;
-        bfinal(P, m, fs == 1u, j, x, lane, d);
-        bprecount(P, m, fs == 2u, j, x, lane, d);
-        const bool stage = ok && fs == 0u;
-        const unsigned b = __ballot_sync(kFull, stage);
-        if (stage) {
-            const uint32_t q0 = nst + __popc(b & ((1u << lane) - 1u));
-            m.stp[q0] = m.pidx_s[j];
-            m.stx[q0] = x;
-            m.stq[q0] = m.qid_s[j];
+#pragma unroll
+        for (uint32_t u = 0; u < kBSlots; u++) {
+            if (!ok[u]) continue;
+            const uint32_t jj = j[u], dj = m.drv_s[jj], k = m.k_s[jj];
+            for (uint32_t i = 0; i < k && ok[u]; i++) {
+                if (i == dj) continue;
+                ok[u] = dev::seg_has_st(m.segs_s[i * 32 + jj], x[u], 1, P.nbr, P.bm, P.bm_words, m.stage);
+            }
+            for (uint32_t c = 0; c < d && ok[u]; c++) ok[u] = m.rows_s[c * 32 + jj] != x[u];
         }
-        nst += __popc(b);
-        if (nst > kBStage - 32) {
+#pragma unroll
+        for (uint32_t u = 0; u < kBSlots; u++) {
+            const uint32_t fs = ok[u] ? m.fin_s[j[u]] : 0u;
+            bfinal(P, m, fs == 1u, j[u], x[u], lane, d);
+            bprecount(P, m, fs == 2u, j[u], x[u], lane, d);
+            const bool stage = ok[u] && fs == 0u;
+            const unsigned b = __ballot_sync(kFull, stage);
+            if (stage) {
+                const uint32_t q0 = nst + __popc(b & ((1u << lane) - 1u));
+                m.stp[q0] = m.pidx_s[j[u]];
+                m.stx[q0] = x[u];
+                m.stq[q0] = m.qid_s[j[u]];
+            }
+            nst += __popc(b);
+        }
+        if (nst > kBStage - 32 * kBSlots) {
             __syncwarp();
             bflush<ROOTS>(P, m, nst, lane, d, chunk);
             nst = 0;
@@ -830,6 +843,45 @@ struct fm_batch {
     uint64_t launches = 0;
     bool impossible_all = false;
     std::vector<uint8_t> impossible;      // a query label absent from the graph
+
+    // Queries matched alone (tuned): a query whose work fills the GPU by
+    // itself gains nothing from sharing launches and, in shared level
+    // buffers, crowds out the others; it runs on the single-query engine
+    // with the whole level memory, after the shared run, its table written
+    // into its own region.  Indices are positions in `batched`.
+    std::vector<uint8_t> solo;
+    std::vector<uint32_t> roots_all;      // n_roots of every batched plan (solo plans get 0 in h_plans)
+    uint32_t n_solo = 0;
+
+    void set_solo(const std::vector<uint8_t>& s) {
+        n_solo = 0;
+        for (size_t i = 0; i < h_plans.size(); i++) {
+            solo[i] = s[i];
+            h_plans[i].n_roots = s[i] ? 0u : roots_all[i];
+            n_solo += s[i] ? 1u : 0u;
+        }
+        plans_dirty = true;
+        drop_graphs();                    // the captured launches bake in the longest root list
+    }
+
+    // The solo queries of one run: counted (count mode, or the counting run
+    // that sizes table regions) or with their tables written into their
+    // regions.  Their counts go to h_qpos like the shared run's.
+    fm_status run_solo(bool tables) {
+        const ContextView cv = context_view(ctx);
+        for (size_t i = 0; i < solo.size(); i++) {
+            if (!solo[i]) continue;
+            const BatchPlan& bp = h_plans[i];
+            const bool tab = tables && !bp.count_only;
+            fm_result r;
+            const fm_status st = match_region(ctx, graph, queries[batched[i]], tab ? FM_MODE_TABLE : FM_MODE_COUNT,
+                                              cv.output + bp.table_base, bp.table_cap, &r);
+            if (st != FM_OK && st != FM_ERR_OUTPUT_OVERFLOW) return st;
+            h_qpos[i] = r.count;
+            launches += r.launches;
+        }
+        return FM_OK;
+    }
 };
 
 namespace {
@@ -1217,6 +1269,8 @@ fm_status batch_create_impl(fm_context* ctx, const fm_graph* graph, const fm_que
         b->cap_floor = (uint64_t)g.max_len * 32 + 32;
         b->layout_levels(cap);
         b->h_plans = plans;
+        b->solo.assign(nq, 0);
+        for (auto& bp : plans) b->roots_all.push_back(bp.n_roots);
         if (scr) {
             // caller-owned scratch: no allocation (a server must not call
             // cudaMalloc/cudaFree while other slots run)
@@ -1319,6 +1373,7 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
             // region of exactly its size (in order, while OUTPUT_PREALLOC lasts).
             run.base.table_mode = 0;
             FM_TRY(run.run(b->replay));
+            FM_TRY(b->run_solo(false));
             const uint64_t words = cv.output_bytes / 4;
             uint64_t off = 0;
             for (uint32_t i = 0; i < nq; i++) {
@@ -1336,6 +1391,7 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
         }
         run.base.table_mode = b->table ? 1u : 0u;
         FM_TRY(run.run(b->replay));
+        FM_TRY(b->run_solo(b->table != 0));
         for (uint32_t i = 0; i < nq; i++) {
             const uint32_t qi = b->batched[i];
             b->counts[qi] = b->h_qpos[i];
@@ -1370,6 +1426,7 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
         stats->persistent = b->persistent ? 1 : 0;
         stats->graph = (b->replay && b->graph_ok) ? 1 : 0;
         stats->weighted_levels = b->weighted ? 1 : 0;
+        stats->solo_queries = (int32_t)b->n_solo;
         for (uint32_t i = 0; i < b->n; i++) stats->embeddings += b->counts[i];
     }
     if (truncated) {
@@ -1480,6 +1537,25 @@ fm_status fm_batch_set_engine(fm_batch* b, int32_t engine) {
     return FM_OK;
 }
 
+fm_status fm_batch_set_solo(fm_batch* b, uint32_t i, int32_t solo) {
+    if (!b || i >= b->n) return FM_ERR_ARG;
+    for (size_t k = 0; k < b->batched.size(); k++) {
+        if (b->batched[k] != i || (b->solo[k] != 0) == (solo != 0)) continue;
+        std::vector<uint8_t> s = b->solo;
+        s[k] = solo ? 1 : 0;
+        b->set_solo(s);
+    }
+    return FM_OK;
+}
+
+fm_status fm_batch_get_solo(const fm_batch* b, uint32_t i, int32_t* solo) {
+    if (!b || i >= b->n || !solo) return FM_ERR_ARG;
+    *solo = 0;
+    for (size_t k = 0; k < b->batched.size(); k++)
+        if (b->batched[k] == i) *solo = b->solo[k];
+    return FM_OK;
+}
+
 fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
     if (!b) return FM_ERR_ARG;
     // Search the split granularity (heavy piece size: the intersection tile a
@@ -1492,6 +1568,53 @@ fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
     // for the level engine the split granularity, a half grid and smaller
     // level buffers.  Each candidate runs the whole batch once (capturing its
     // graph, which the run then launches) and is timed on that run.
+    //
+    // First the queries matched alone: every batched query is timed alone on
+    // the single-query engine, and a query runs alone when that time is at
+    // least a threshold (8 ms or 2 ms: its work fills the GPU by itself);
+    // the threshold with the fastest run is kept (or none).  The engine and
+    // level-buffer search below then runs with that set.
+    if (b->replay && !b->batched.empty()) {      // a server's batches share their launches
+        const size_t nb = b->batched.size();
+        b->set_solo(std::vector<uint8_t>(nb, 0));
+        b->layout_levels(b->cap_full >> b->bank_shift);
+        fm_batch_stats st0;
+        fm_status s0 = fm_batch_run(b, nullptr, &st0);    // sizes the table regions, captures
+        if (s0 != FM_OK && s0 != FM_ERR_OUTPUT_OVERFLOW) return s0;
+        s0 = fm_batch_run(b, nullptr, &st0);
+        if (s0 != FM_OK && s0 != FM_ERR_OUTPUT_OVERFLOW) return s0;
+        const ContextView cv = context_view(b->ctx);
+        std::vector<double> alone(nb, 0.0);
+        for (size_t i = 0; i < nb; i++) {
+            const BatchPlan& bp = b->h_plans[i];
+            const bool tab = b->table && !bp.count_only;
+            fm_result r;
+            const fm_status st = match_region(b->ctx, b->graph, b->queries[b->batched[i]],
+                                              tab ? FM_MODE_TABLE : FM_MODE_COUNT, cv.output + bp.table_base,
+                                              bp.table_cap, &r);
+            if (st != FM_OK && st != FM_ERR_OUTPUT_OVERFLOW) return st;
+            alone[i] = r.device_ms;
+        }
+        double solo_best = st0.wall_ms;
+        std::vector<uint8_t> solo_pick(nb, 0);
+        for (const double tau : {8.0, 2.0}) {
+            std::vector<uint8_t> sv(nb, 0);
+            bool any = false;
+            for (size_t i = 0; i < nb; i++) any |= (sv[i] = alone[i] >= tau ? 1 : 0) != 0;
+            if (!any || sv == solo_pick) continue;
+            b->set_solo(sv);
+            fm_batch_stats st;
+            fm_status s1 = fm_batch_run(b, nullptr, &st);     // captures the shared part
+            if (s1 != FM_OK && s1 != FM_ERR_OUTPUT_OVERFLOW) return s1;
+            s1 = fm_batch_run(b, nullptr, &st);
+            if (s1 != FM_OK && s1 != FM_ERR_OUTPUT_OVERFLOW) return s1;
+            if (st.wall_ms < solo_best) {
+                solo_best = st.wall_ms;
+                solo_pick = sv;
+            }
+        }
+        b->set_solo(solo_pick);
+    }
     struct Cand {
         bool persistent;
         uint32_t shift, quarters, bank;
@@ -1553,6 +1676,7 @@ fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
         best->persistent = b->persistent ? 1 : 0;
         best->graph = b->graph_ok ? 1 : 0;
         best->weighted_levels = b->weighted ? 1 : 0;
+        best->solo_queries = (int32_t)b->n_solo;
     }
     return FM_OK;
 }

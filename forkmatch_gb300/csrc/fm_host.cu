@@ -771,12 +771,12 @@ __global__ void k_iota_rows(uint32_t* out, uint64_t n, uint32_t first, uint64_t 
 
 }  // namespace
 
-extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_query* query,
-                              const fm_match_opts* opts_in, fm_result* out) {
-    if (!ctx || !graph || !query || !out) return FM_ERR_ARG;
-    fm_match_opts opts;
-    if (opts_in) opts = *opts_in;
-    else fm_match_opts_default(&opts);
+namespace {
+
+// fm_match with the table written into `region` (device memory, `region_rows`
+// rows) instead of the start of OUTPUT_PREALLOC when `region` is set.
+fm_status match_impl(fm_context* ctx, const fm_graph* graph, const fm_query* query, const fm_match_opts& opts,
+                     fm_result* out, uint32_t* region, uint64_t region_rows) {
     std::memset(out, 0, sizeof(*out));
     const DeviceGraph& g = graph->g;
     const Plan& pl = query->p;
@@ -799,8 +799,8 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     // The table lives in the context's OUTPUT_PREALLOC region, or -- host_direct --
     // in the caller's pinned host buffer, written by the kernels over the host link.
     const bool direct = table && opts.host_direct && opts.host_rows;
-    uint32_t* table_ptr = ctx->output;
-    uint64_t table_cap = ctx->output_bytes / (4ull * q);
+    uint32_t* table_ptr = region ? region : ctx->output;
+    uint64_t table_cap = region ? region_rows : ctx->output_bytes / (4ull * q);
     if (direct) {
         cudaPointerAttributes a;
         if (cudaPointerGetAttributes(&a, opts.host_rows) != cudaSuccess || a.type != cudaMemoryTypeHost ||
@@ -957,13 +957,13 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
     if (q > 1) out->count = table ? ctx->h_tot->table_pos : ctx->h_tot->count;
     out->rows = table ? std::min<uint64_t>(out->count, table_cap) : 0;
     out->truncated = table && out->count > table_cap;
-    out->rows_device = (table && !direct) ? ctx->output : nullptr;
+    out->rows_device = (table && !direct) ? table_ptr : nullptr;
     if (q > 1) out->level[q - 1].produced = out->count;
     if (direct) {
         out->rows_copied = out->rows;   // already in host memory
     } else if (table && opts.host_rows && out->rows) {
         uint64_t n = std::min<uint64_t>(out->rows, opts.host_rows_cap);
-        FM_CUDA(cudaMemcpyAsync(opts.host_rows, ctx->output, n * q * 4, cudaMemcpyDeviceToHost, s));
+        FM_CUDA(cudaMemcpyAsync(opts.host_rows, table_ptr, n * q * 4, cudaMemcpyDeviceToHost, s));
         FM_CUDA(cudaStreamSynchronize(s));
         out->rows_copied = n;
     }
@@ -978,6 +978,25 @@ extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_q
         return FM_ERR_OUTPUT_OVERFLOW;
     }
     return FM_OK;
+}
+
+}  // namespace
+
+extern "C" fm_status fm_match(fm_context* ctx, const fm_graph* graph, const fm_query* query,
+                              const fm_match_opts* opts_in, fm_result* out) {
+    if (!ctx || !graph || !query || !out) return FM_ERR_ARG;
+    fm_match_opts opts;
+    if (opts_in) opts = *opts_in;
+    else fm_match_opts_default(&opts);
+    return match_impl(ctx, graph, query, opts, out, nullptr, 0);
+}
+
+fm_status fm::match_region(fm_context* ctx, const fm_graph* graph, const fm_query* query, int32_t mode,
+                           uint32_t* region, uint64_t region_rows, fm_result* out) {
+    fm_match_opts opts;
+    fm_match_opts_default(&opts);
+    opts.mode = mode;
+    return match_impl(ctx, graph, query, opts, out, mode == FM_MODE_TABLE ? region : nullptr, region_rows);
 }
 
 fm_status fm::context_create_view(fm_context* owner, char* misc, fm_context** out) {

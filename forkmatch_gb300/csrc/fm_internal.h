@@ -251,6 +251,11 @@ uint32_t stage_words_knob();
 // Count the last depth from depth q-2 when it has one back edge (FM_PRE_COUNT,
 // default 1; 0 launches the last depth as its own level).
 bool pre_count_knob();
+// One query matched alone on the context's stream (the single-query engine),
+// its table (FM_MODE_TABLE) written into `region`, a device buffer of
+// `region_rows` rows; used by batches for the queries they match alone.
+fm_status match_region(fm_context* ctx, const fm_graph* graph, const fm_query* query, int32_t mode,
+                       uint32_t* region, uint64_t region_rows, fm_result* out);
 int persist_blocks_per_sm(int last_mode, bool dups, size_t smem);
 cudaError_t launch_persist(const ExpandParams& p, const PersistArgs& a, int last_mode, bool dups, int grid,
                            size_t smem, cudaStream_t s);

@@ -274,7 +274,8 @@ typedef struct fm_batch_stats {
     int32_t persistent;         /* 1: one cooperative launch per run (FM_ENGINE_PERSISTENT) */
     int32_t graph;              /* 1: the run is a captured CUDA graph replay */
     int32_t weighted_levels;    /* 1: level buffers sized from the previous run's per-depth volumes */
-    int32_t reserved;
+    int32_t solo_queries;       /* tuned: queries matched alone inside the run (the single-query
+                                   engine with the whole level memory, table into their region) */
 } fm_batch_stats;
 
 fm_status fm_batch_create(fm_context* ctx, const fm_graph* g, const fm_query* const* queries, uint32_t n,
@@ -300,9 +301,21 @@ fm_status fm_batch_set_query_mode(fm_batch* b, uint32_t i, int32_t mode);
 /* Engine of later runs: an fm_engine value, FM_ENGINE_LEVELS by default;
  * fm_batch_tune picks the faster one.  Results do not depend on it. */
 fm_status fm_batch_set_engine(fm_batch* b, int32_t engine);
-/* Autotuner: runs the batch under each candidate engine, split granularity
- * (the intersection tile a warp walks), grid (warps in flight per SM) and
- * level buffer size (the bank size), keeps the fastest for later runs. */
+/* Query i matched alone inside later runs (solo != 0): on the single-query
+ * engine with the whole level memory, after the shared launches, its table
+ * in its own region; or back in the shared launches (solo == 0).  Results do
+ * not depend on it.  fm_batch_tune picks the queries whose work fills the GPU
+ * by themselves; fm_batch_get_solo reads the choice, so that a later batch of
+ * the same queries can reuse it without tuning.  Queries matched on their own
+ * for other reasons (one vertex, duplicate e-lines) are unaffected. */
+fm_status fm_batch_set_solo(fm_batch* b, uint32_t i, int32_t solo);
+fm_status fm_batch_get_solo(const fm_batch* b, uint32_t i, int32_t* solo);
+/* Autotuner: first times every query alone and keeps the set of queries
+ * matched alone (those at or above 8 ms or 2 ms alone, or none) with the
+ * fastest run; then runs the batch under each candidate engine, split
+ * granularity (the intersection tile a warp walks), grid (warps in flight
+ * per SM) and level buffer size (the bank size), keeps the fastest for later
+ * runs. */
 fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best);
 void fm_batch_free(fm_batch* b);
 

@@ -190,3 +190,34 @@ def test_batch_with_list_bitmaps(monkeypatch):
     b.close()
     g.close()
     ctx.close()
+
+
+def test_batch_solo_queries_keep_counts_and_tables(env):
+    """Queries matched alone inside a run (the single-query engine, table into
+    the query's own region) give the same counts and tables as the shared
+    launches, in count and table mode, on captured runs and replays, with
+    every query alone, some, and back to none; the tuner's choice (read back
+    with solo()) keeps them too."""
+    ctx, g, og, queries, texts, want = env
+    tabled = [i for i, w in enumerate(want) if w <= 1 << 18]
+    singles = {i: fm.match_table(ctx, g, queries[i], max_rows=max(1, want[i]))[1] for i in tabled}
+    for mode in (fm.MODE_COUNT, fm.MODE_TABLE):
+        b = fm.Batch(ctx, g, queries, mode=mode)
+        if mode == fm.MODE_TABLE:
+            for i in range(len(queries)):
+                if i not in tabled:
+                    b.set_query_mode(i, fm.MODE_COUNT)
+        for pick in (list(range(len(queries))), [0, 3, 6, 7, 11], []):
+            for i in range(len(queries)):
+                b.set_solo(i, i in pick)
+            assert b.solo() == pick
+            for _ in range(2):
+                counts, st = b.run()
+                assert counts == want and st.solo_queries == len(pick)
+            if mode == fm.MODE_TABLE:
+                for i in tabled:
+                    assert np.array_equal(_sorted(b.rows(i, max(1, want[i]))), _sorted(singles[i])), (pick, i)
+        best = b.tune()
+        assert best.solo_queries == len(b.solo())
+        assert b.run()[0] == want
+        b.close()
