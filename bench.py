@@ -62,6 +62,10 @@ def parse_args():
     ap.add_argument("--ncu-step", action="store_true",
                     help="run one untimed step with small knobs (SOLN 2 GiB, OUTPUT 4.5 GiB) for ncu captures")
     ap.add_argument("--queries", default="all", help="with --ncu-step: comma-separated query indices")
+    ap.add_argument("--ncu-scale", type=int, default=0,
+                    help="with --ncu-step --workload batched: match on an R-MAT graph of 2^N vertices and 16 * 2^N "
+                         "edges with the workload's generator parameters instead of the full graph (counts "
+                         "are not checked)")
     # serving workload
     ap.add_argument("--serving-scale", type=int, default=24, help="log2 vertices (edges scale along)")
     ap.add_argument("--serving-queries", type=int, default=128)
@@ -113,7 +117,16 @@ def run_ncu_step(args):
         g.close()
         ctx.close()
         return 0
-    wl, G, (src, dst, lab), same, _ = load_workload(args.workload)
+    if args.ncu_scale and args.workload == "batched":
+        from forkmatch_gb300 import synth as S
+        from forkmatch_gb300 import workloads as W
+        wl = W.load_workload("batched")
+        p = W.BATCHED
+        G = S.rmat(args.ncu_scale, 16 << args.ncu_scale, p["seed"], p["n_elabels"])
+        src, dst, lab = G.directed()
+        same = False
+    else:
+        wl, G, (src, dst, lab), same, _ = load_workload(args.workload)
     pick = None if args.queries == "all" else {int(x) for x in args.queries.split(",")}
     # the table region only as large as the picked table queries need
     need = sum(q["count"] * query_vertices(q) * 4 for i, q in enumerate(wl["queries"])
@@ -567,18 +580,25 @@ def batched_config(wl, G, same):
             "l2": "inputs larger than L2: resident graph 5.7 GB vs 129 MB L2; no flush between steps"}
 
 
-def batched_traffic(alg_bytes):
+def batched_traffic(alg_shared, alg_alone):
     """DRAM bytes of one batch run: the ncu summary's DRAM bytes per
-    algorithmic byte (captured on a smaller batch of the same kernels) times
-    this run's algorithmic bytes."""
+    algorithmic byte (captured on a smaller batch of the same queries) times
+    this run's algorithmic bytes, separately for the queries in the shared
+    launches (batch kernels) and the queries matched alone (single-query
+    kernels)."""
     p = os.path.join(ROOT, "profiles", "k_bexpand_batched.md")
+    ratio = {}
     try:
         for line in open(p):
-            if line.startswith("traffic_bytes_per_algorithmic_byte:"):
-                return int(alg_bytes * float(line.split(":")[1]))
+            for key in ("traffic_bytes_per_algorithmic_byte", "traffic_bytes_per_algorithmic_byte_single"):
+                if line.startswith(key + ":"):
+                    ratio[key] = float(line.split(":")[1])
     except (OSError, ValueError):
-        pass
-    return None
+        return None
+    if len(ratio) < 2:
+        return None
+    return int(alg_shared * ratio["traffic_bytes_per_algorithmic_byte"] +
+               alg_alone * ratio["traffic_bytes_per_algorithmic_byte_single"])
 
 
 def allreduce_counts_and_times(counts, times):
@@ -652,7 +672,8 @@ def run_batched(args, rank, world, local):
     # order in both forms), from the plain form's per-level counters
     prof = []
     plain_step(collect=prof, profile=True)
-    alg_bytes = sum(match_alg_bytes(r, qi, c_only) for r, qi, c_only in zip(prof, qinfo, counted))
+    alg_each = [match_alg_bytes(r, qi, c_only) for r, qi, c_only in zip(prof, qinfo, counted)]
+    alg_bytes = sum(alg_each)
 
     b = fm.Batch(ctx, g, queries, mode=fm.MODE_TABLE)
     for i, c_only in enumerate(counted):
@@ -709,6 +730,7 @@ def run_batched(args, rank, world, local):
     # a later batch of the same queries reuses the tuner's choices that are
     # per query or per engine (the queries matched alone, the engine)
     solo_idx = b.solo()
+    alg_alone = sum(alg_each[i] for i in solo_idx)
 
     def e2e_fresh():
         qs = [fm.Query.from_text(tx) for tx in texts]
@@ -782,11 +804,14 @@ def run_batched(args, rank, world, local):
                       "batched_queries": st.batched_queries, "single_queries": st.single_queries,
                       "solo_queries": st.solo_queries},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": batched_traffic(alg_bytes / max(1, world)),
+                         "frac": achieved / peak,
+                         "traffic": batched_traffic(alg_bytes / max(1, world) - alg_alone, alg_alone),
                          "kernel": "k_bexpand + k_bexpand_heavy (one batch run; k_bpersist when the tuner picks the persistent engine)",
                          "peak_kind": peak_kind, "algorithmic_bytes_per_step": alg_bytes,
-                         "traffic_source": "profiles/k_bexpand_batched.md (DRAM bytes per algorithmic byte, "
-                                           "scaled to one batch run)",
+                         "traffic_source": "profiles/k_bexpand_batched.md (DRAM bytes per algorithmic byte of "
+                                           "the batch kernels and of the single-query kernels, captured on every "
+                                           "32nd query at 2^20 vertices, applied to this run's shared and alone "
+                                           "queries)",
                          "note": "achieved = algorithmic bytes of all queries / device time of one batch run"},
             "cpu_baseline": cpu,
             "e2e_paths": e2e_paths, "e2e": e2e,

@@ -317,9 +317,15 @@ fm_status build_device_graph(DeviceGraph& g, uint32_t V, uint32_t L, uint64_t E,
 
         // membership bitmaps for the longest lists (not with duplicates: a
         // bit cannot count copies; vertex ids must leave bit 31 of z free)
-        const uint64_t budget = env_bytes("FM_BITMAP_BYTES", 2ull << 30);
-        const uint64_t min_len = std::max<uint64_t>(4, env_bytes("FM_BITMAP_MIN_LEN", 64));
+        // default budget: room for 16384 bitmaps, between 2 and 8 GiB (on a
+        // 2^22-vertex R-MAT graph with 64 labels, 8 GiB covers its 16256
+        // lists of 256+ entries and measured faster than 2 GiB for every
+        // query class, while 61 GB of bitmaps down to 64 entries slowed the
+        // table queries)
         const uint32_t words = (V + 31) / 32;
+        const uint64_t budget = env_bytes(
+            "FM_BITMAP_BYTES", std::min<uint64_t>(8ull << 30, std::max<uint64_t>(2ull << 30, 16384ull * 4ull * words)));
+        const uint64_t min_len = std::max<uint64_t>(4, env_bytes("FM_BITMAP_MIN_LEN", 64));
         const uint64_t cap64 = budget / (4ull * words);
         if (!dup_seen && V < kBitmapMark && cap64 > 0 && nlong_hint(d_nlong, s) > 0) {
             uint32_t min_log2 = 0;

@@ -90,7 +90,8 @@ void* fm_context_stream(fm_context* ctx);
  * resident graph serves every context on the same device.  The longest lists
  * also get a bitmap over all vertices (membership in one load instead of a
  * binary search) while the bitmaps fit FM_BITMAP_BYTES (environment, default
- * 2 GiB; 0 disables) and are at least FM_BITMAP_MIN_LEN (default 64) long;
+ * room for 16384 bitmaps of V bits, within 2..8 GiB; 0 disables) and are at
+ * least FM_BITMAP_MIN_LEN (default 64) long;
  * graphs with duplicate e-lines get none. */
 typedef struct fm_graph fm_graph;
 typedef struct fm_graph_info {
