@@ -170,7 +170,8 @@ constexpr uint32_t kBStageSpinLimit = 1u << 22;
 // Stage the membership lists of a loaded chunk into the warp's stage with
 // TMA bulk copies (the same rule as the single-query kernel, with each lane's
 // own number of back edges k and driver drv): non-driver lists of
-// 4..kBStageMaxList entries without a bitmap, for parents with at least two
+// 4..kBStageMaxList entries without a bitmap whose copy pays for itself by
+// the list-length ratio (dev::stage_worth), for parents with at least two
 // candidates, lanes in order while the stage has room.  Returns false
 // (warp-uniform) if the bounded wait ran out; error bit 2 is then raised.
 __device__ __forceinline__ bool bstage_lists(const BatchParams& P, const BMem& m, uint32_t lane, uint32_t k,
@@ -180,7 +181,7 @@ __device__ __forceinline__ bool bstage_lists(const BatchParams& P, const BMem& m
         for (uint32_t i = 0; i < k; i++) {
             if (i == drv) continue;
             const uint4 r = m.segs_s[i * 32 + lane];
-            if (r.x > 3 && r.x <= kBStageMaxList && !(r.z & kBitmapMark)) want += (r.x + 3) & ~3u;
+            if (dev::stage_worth(r, n, kBStageMaxList)) want += (r.x + 3) & ~3u;
         }
     }
     uint32_t incl = want;
@@ -203,7 +204,7 @@ __device__ __forceinline__ bool bstage_lists(const BatchParams& P, const BMem& m
         for (uint32_t i = 0; i < k; i++) {
             if (i == drv) continue;
             uint4 r = m.segs_s[i * 32 + lane];
-            if (r.x > 3 && r.x <= kBStageMaxList && !(r.z & kBitmapMark)) {
+            if (dev::stage_worth(r, n, kBStageMaxList)) {
                 const uint32_t words = (r.x + 3) & ~3u;
                 dev::bulk_copy_g2s(m.stage + off, P.nbr + (uint64_t)r.y * 4, words * 4, m.mbar);
                 r.y = dev::kStagedMark | off;

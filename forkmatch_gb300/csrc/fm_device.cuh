@@ -193,6 +193,20 @@ __device__ __forceinline__ uint32_t lower_bound_s(const uint32_t* a, uint32_t n,
     return lo;
 }
 
+// Intersection method of one membership list, chosen per parent by the
+// list-length ratio: a list of n entries probed by the m candidates of the
+// parent's driver list is copied into the warp's shared-memory stage (a TMA
+// bulk copy, then binary searches in shared memory) when the candidates'
+// searches in global memory, about m * ceil(log2 n) dependent loads, outweigh
+// copying its n / 32 128-byte lines; with a more skewed ratio each candidate
+// searches the list in global memory.  Inline lists (<= 3 entries) compare in
+// registers and bitmap lists take one load, so neither is staged.
+__device__ __forceinline__ bool stage_worth(const uint4& r, uint32_t m, uint32_t max_list) {
+    if (r.x <= 3 || r.x > max_list || (r.z & kBitmapMark)) return false;
+    const uint32_t lg = 32u - __clz(r.x - 1u);
+    return (unsigned long long)m * 32u * lg >= r.x;
+}
+
 // seg_has for records that may point into the warp's stage.
 __device__ __forceinline__ bool seg_has_st(const uint4& s, uint32_t x, uint32_t need, const uint32_t* __restrict__ nbr,
                                            const uint32_t* __restrict__ bm, uint32_t bm_words, const uint32_t* stage) {

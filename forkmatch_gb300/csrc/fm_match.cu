@@ -170,8 +170,9 @@ constexpr uint32_t kStageMaxList = 2048;
 constexpr uint32_t kStageSpinLimit = 1u << 22;
 
 // Stage the membership lists of the loaded chunk: every lane's non-driver
-// lists of 4..kStageMaxList entries without a bitmap, when its parent has at
-// least two candidates, are copied into the warp's stage with TMA bulk copies
+// lists of 4..kStageMaxList entries without a bitmap that its parent's
+// candidates probe often enough for the copy to pay (the list-length ratio
+// rule of dev::stage_worth) are copied into the warp's stage with TMA bulk copies
 // (lanes in order while the stage has room) and their records in segs_s are
 // pointed at the stage.  Lane 0 arms the barrier with the byte count, every
 // lane issues its own copies, and the warp waits for the phase, boundedly.
@@ -184,7 +185,7 @@ __device__ __forceinline__ bool stage_lists(const ExpandParams& P, const WarpMem
         for (uint32_t i = 0; i < k; i++) {
             if (i == drv) continue;
             const uint4 r = m.segs_s[i * 32 + lane];
-            if (r.x > 3 && r.x <= kStageMaxList && !(r.z & kBitmapMark)) want += (r.x + 3) & ~3u;
+            if (dev::stage_worth(r, n, kStageMaxList)) want += (r.x + 3) & ~3u;
         }
     }
     uint32_t incl = want;
@@ -208,7 +209,7 @@ __device__ __forceinline__ bool stage_lists(const ExpandParams& P, const WarpMem
         for (uint32_t i = 0; i < k; i++) {
             if (i == drv) continue;
             uint4 r = m.segs_s[i * 32 + lane];
-            if (r.x > 3 && r.x <= kStageMaxList && !(r.z & kBitmapMark)) {
+            if (dev::stage_worth(r, n, kStageMaxList)) {
                 const uint32_t words = (r.x + 3) & ~3u;
                 dev::bulk_copy_g2s(m.stage + off, P.nbr + (uint64_t)r.y * 4, words * 4, m.mbar);
                 r.y = dev::kStagedMark | off;
