@@ -868,11 +868,12 @@ struct fm_batch {
     // The solo queries of one run: counted (count mode, or the counting run
     // that sizes table regions) or with their tables written into their
     // regions.  Their counts go to h_qpos like the shared run's.
-    fm_status run_solo(bool tables) {
+    fm_status run_solo(bool tables, bool skip_count_only = false) {
         const ContextView cv = context_view(ctx);
         for (size_t i = 0; i < solo.size(); i++) {
             if (!solo[i]) continue;
             const BatchPlan& bp = h_plans[i];
+            if (skip_count_only && bp.count_only) continue;
             const bool tab = tables && !bp.count_only;
             fm_result r;
             const fm_status st = match_region(ctx, graph, queries[batched[i]], tab ? FM_MODE_TABLE : FM_MODE_COUNT,
@@ -1369,6 +1370,8 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
                                     cv.stream));
             b->plans_dirty = false;
         }
+        bool skip_counted = false;
+        std::vector<uint64_t> first_counts;
         if (b->table && !b->regions_exact) {
             // First table run: count every query, then give each query a table
             // region of exactly its size (in order, while OUTPUT_PREALLOC lasts).
@@ -1386,13 +1389,31 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
                 b->table_base[i] = bp.table_base;
                 b->table_cap[i] = bp.table_cap;
             }
+            // The counting run left the count-only queries' counts exact: the
+            // table run that follows skips them (their roots withheld), and
+            // their counts are kept.  That run is launched directly, not
+            // captured, since its plans differ from later runs'.
+            for (uint32_t i = 0; i < nq; i++) {
+                if (!b->h_plans[i].count_only) continue;
+                if (!skip_counted) first_counts.assign(b->h_qpos, b->h_qpos + nq);
+                skip_counted = true;
+                b->h_plans[i].n_roots = 0;
+            }
             FM_CUDA(cudaMemcpyAsync(b->d_plans, b->h_plans.data(), nq * sizeof(BatchPlan), cudaMemcpyHostToDevice,
                                     cv.stream));
             b->regions_exact = true;
         }
         run.base.table_mode = b->table ? 1u : 0u;
-        FM_TRY(run.run(b->replay));
-        FM_TRY(b->run_solo(b->table != 0));
+        FM_TRY(run.run(b->replay && !skip_counted));
+        FM_TRY(b->run_solo(b->table != 0, skip_counted));
+        if (skip_counted) {
+            for (uint32_t i = 0; i < nq; i++) {
+                if (!b->h_plans[i].count_only) continue;
+                b->h_qpos[i] = first_counts[i];
+                b->h_plans[i].n_roots = b->solo[i] ? 0u : b->roots_all[i];
+            }
+            b->plans_dirty = true;
+        }
         for (uint32_t i = 0; i < nq; i++) {
             const uint32_t qi = b->batched[i];
             b->counts[qi] = b->h_qpos[i];
