@@ -868,12 +868,13 @@ struct fm_batch {
     // The solo queries of one run: counted (count mode, or the counting run
     // that sizes table regions) or with their tables written into their
     // regions.  Their counts go to h_qpos like the shared run's.
-    fm_status run_solo(bool tables, bool skip_count_only = false) {
+    enum class SoloPick { All, CountOnly };
+    fm_status run_solo(bool tables, SoloPick pick = SoloPick::All) {
         const ContextView cv = context_view(ctx);
         for (size_t i = 0; i < solo.size(); i++) {
             if (!solo[i]) continue;
             const BatchPlan& bp = h_plans[i];
-            if (skip_count_only && bp.count_only) continue;
+            if (pick == SoloPick::CountOnly && !bp.count_only) continue;
             const bool tab = tables && !bp.count_only;
             fm_result r;
             const fm_status st = match_region(ctx, graph, queries[batched[i]], tab ? FM_MODE_TABLE : FM_MODE_COUNT,
@@ -1370,45 +1371,69 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
                                     cv.stream));
             b->plans_dirty = false;
         }
-        bool skip_counted = false;
+        // done[i]: query i's result is already final in this (first table) run
+        std::vector<uint8_t> done;
         std::vector<uint64_t> first_counts;
         if (b->table && !b->regions_exact) {
-            // First table run: count every query, then give each query a table
-            // region of exactly its size (in order, while OUTPUT_PREALLOC lasts).
+            // First table run: count the queries of the shared launches and
+            // the count-only queries matched alone, give each shared table
+            // query a table region of exactly its size (in order, while
+            // OUTPUT_PREALLOC lasts), then match the table queries matched
+            // alone in table mode once, each straight into the free space
+            // after the last region (its region is what it wrote).
             run.base.table_mode = 0;
             FM_TRY(run.run(b->replay));
-            FM_TRY(b->run_solo(false));
+            FM_TRY(b->run_solo(false, fm_batch::SoloPick::CountOnly));
             const uint64_t words = cv.output_bytes / 4;
             uint64_t off = 0;
             for (uint32_t i = 0; i < nq; i++) {
                 BatchPlan& bp = b->h_plans[i];
+                if (b->solo[i] && !bp.count_only) continue;
                 const uint64_t need = bp.count_only ? 0 : b->h_qpos[i] * bp.q;
                 bp.table_base = off;
                 bp.table_cap = (!bp.count_only && off + need <= words) ? b->h_qpos[i] : 0;
                 off += bp.table_cap * bp.q;
-                b->table_base[i] = bp.table_base;
-                b->table_cap[i] = bp.table_cap;
             }
-            // The counting run left the count-only queries' counts exact: the
-            // table run that follows skips them (their roots withheld), and
-            // their counts are kept.  That run is launched directly, not
-            // captured, since its plans differ from later runs'.
             for (uint32_t i = 0; i < nq; i++) {
-                if (!b->h_plans[i].count_only) continue;
-                if (!skip_counted) first_counts.assign(b->h_qpos, b->h_qpos + nq);
-                skip_counted = true;
-                b->h_plans[i].n_roots = 0;
+                BatchPlan& bp = b->h_plans[i];
+                if (!b->solo[i] || bp.count_only) continue;
+                bp.table_base = off;
+                bp.table_cap = (words - off) / bp.q;
+                fm_result r;
+                const fm_status st = match_region(b->ctx, b->graph, b->queries[b->batched[i]], FM_MODE_TABLE,
+                                                  cv.output + off, bp.table_cap, &r);
+                if (st != FM_OK && st != FM_ERR_OUTPUT_OVERFLOW) return st;
+                b->launches += r.launches;
+                b->h_qpos[i] = r.count;
+                bp.table_cap = std::min<uint64_t>(bp.table_cap, r.count);
+                off += bp.table_cap * bp.q;
+            }
+            for (uint32_t i = 0; i < nq; i++) {
+                b->table_base[i] = b->h_plans[i].table_base;
+                b->table_cap[i] = b->h_plans[i].table_cap;
+            }
+            // Count-only queries are exact after the counting run and the
+            // table queries matched alone are written: the table pass below
+            // skips both (shared ones by withholding their roots; it is
+            // launched directly, not captured, since its plans differ from
+            // later runs').
+            first_counts.assign(b->h_qpos, b->h_qpos + nq);
+            done.assign(nq, 0);
+            for (uint32_t i = 0; i < nq; i++) {
+                done[i] = (b->h_plans[i].count_only || b->solo[i]) ? 1 : 0;
+                if (b->h_plans[i].count_only) b->h_plans[i].n_roots = 0;
             }
             FM_CUDA(cudaMemcpyAsync(b->d_plans, b->h_plans.data(), nq * sizeof(BatchPlan), cudaMemcpyHostToDevice,
                                     cv.stream));
             b->regions_exact = true;
         }
         run.base.table_mode = b->table ? 1u : 0u;
-        FM_TRY(run.run(b->replay && !skip_counted));
-        FM_TRY(b->run_solo(b->table != 0, skip_counted));
-        if (skip_counted) {
+        FM_TRY(run.run(b->replay && done.empty()));
+        if (done.empty()) {
+            FM_TRY(b->run_solo(b->table != 0, fm_batch::SoloPick::All));
+        } else {
             for (uint32_t i = 0; i < nq; i++) {
-                if (!b->h_plans[i].count_only) continue;
+                if (!done[i]) continue;
                 b->h_qpos[i] = first_counts[i];
                 b->h_plans[i].n_roots = b->solo[i] ? 0u : b->roots_all[i];
             }
@@ -1510,8 +1535,8 @@ fm_status fm_batch_copy_tables(const fm_batch* b, uint32_t* host, uint64_t cap_w
     if (offsets)
         for (uint32_t i = 0; i < b->n; i++) offsets[i] = UINT64_MAX;
     if (!b->table || b->batched.empty()) return FM_OK;
-    // regions are laid out in batch order; the packed span ends after the last
-    // region that holds rows
+    // regions are disjoint; the packed span ends after the last region that
+    // holds rows
     uint64_t end = 0;
     for (size_t k = 0; k < b->batched.size(); k++) {
         const uint32_t qi = b->batched[k];

@@ -261,7 +261,9 @@ fm_status fm_match(fm_context* ctx, const fm_graph* g, const fm_query* q,
  * size in OUTPUT_PREALLOC, in batch order while it lasts (a query that does
  * not fit gets FM_ERR_OUTPUT_OVERFLOW; counts stay exact); queries set to
  * count only keep the counts of that counting run and are not matched again
- * in the first run's table pass.  Queries with one
+ * in the first run's table pass, and table queries matched alone
+ * (fm_batch_set_solo) are matched once, in table mode, each into the free
+ * space after the last region.  Queries with one
  * vertex, and every query on a graph with duplicate e-lines, are matched one
  * by one through fm_match (count only). */
 typedef struct fm_batch fm_batch;
