@@ -1605,22 +1605,20 @@ fm_status fm_batch_get_solo(const fm_batch* b, uint32_t i, int32_t* solo) {
 
 fm_status fm_batch_tune(fm_batch* b, fm_batch_stats* best) {
     if (!b) return FM_ERR_ARG;
-    // Search the split granularity (heavy piece size: the intersection tile a
-    // warp walks), the grid (warps in flight per SM) and the level-buffer
-    // size (rows per buffer, the bank size: small buffers keep the rows of a
-    // depth-first drain in L2, large ones need fewer passes); keep the
-    // fastest.  Each configuration runs the whole batch twice (capture, then
-    // the timed replay).
-    // Candidates: both engines at the full grid and full level buffers, then
-    // for the level engine the split granularity, a half grid and smaller
-    // level buffers.  Each candidate runs the whole batch once (capturing its
-    // graph, which the run then launches) and is timed on that run.
-    //
     // First the queries matched alone: every batched query is timed alone on
     // the single-query engine, and a query runs alone when that time is at
     // least a threshold (8 ms or 2 ms: its work fills the GPU by itself);
-    // the threshold with the fastest run is kept (or none).  The engine and
-    // level-buffer search below then runs with that set.
+    // each threshold's batch is timed on a replay after its capturing run,
+    // and the fastest set (possibly none) is kept.
+    // Then, with that set, the engine, the split granularity (heavy piece
+    // size: the intersection tile a warp walks), the grid (warps in flight
+    // per SM) and the level-buffer size (rows per buffer, the bank size:
+    // small buffers keep the rows of a depth-first drain in L2, large or
+    // volume-weighted ones need fewer passes): both engines at the full grid
+    // and full level buffers, then for the level engine the split
+    // granularity, a half grid, smaller and volume-weighted level buffers.
+    // Each candidate runs the whole batch once (capturing its graph, which
+    // that run then launches) and is timed on that run; the fastest is kept.
     if (b->replay && !b->batched.empty()) {      // a server's batches share their launches
         const size_t nb = b->batched.size();
         b->set_solo(std::vector<uint8_t>(nb, 0));
