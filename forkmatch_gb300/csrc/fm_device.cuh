@@ -10,14 +10,6 @@ constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ uint4 ldg4(const uint4* p) { return __ldg(p); }
 
-// Sum of one u32 per lane over the full warp, exact (two 16-bit halves, each
-// sum below 2^21).
-__device__ __forceinline__ unsigned long long warp_sum_u32(uint32_t v) {
-    const unsigned lo = __reduce_add_sync(kFull, v & 0xffffu);
-    const unsigned hi = __reduce_add_sync(kFull, v >> 16);
-    return ((unsigned long long)hi << 16) + lo;
-}
-
 // Element t of a (label, vertex) list given its segment record.
 __device__ __forceinline__ uint32_t seg_at(const uint4& s, uint32_t t, const uint32_t* __restrict__ nbr) {
     if (s.x <= 3) return t == 0 ? s.y : (t == 1 ? s.z : s.w);
@@ -44,7 +36,10 @@ __device__ __forceinline__ uint32_t lower_bound_g(const uint32_t* __restrict__ a
 __device__ __forceinline__ bool seg_has(const uint4& s, uint32_t x, uint32_t need, const uint32_t* __restrict__ nbr,
                                         const uint32_t* __restrict__ bm, uint32_t bm_words) {
     if (s.x <= 3) {
-        const uint32_t c = (s.x > 0 && s.y == x) + (s.x > 1 && s.z == x) + (s.x > 2 && s.w == x);
+        // an empty list's record is all zero; in a non-empty one the unused
+        // inline slots hold kNoVertex, which no vertex id equals
+        if (s.x == 0) return false;
+        const uint32_t c = (s.y == x) + (s.z == x) + (s.w == x);
         return c >= need;
     }
     if (x > s.w) return false;
@@ -75,9 +70,10 @@ __device__ __forceinline__ uint32_t count_members(const uint4& s, const uint32_t
     uint32_t found = 0;
     if (s.x == 0) return 0;
     if (s.x <= 3) {
+        // s.x >= 1 here; unused inline slots hold kNoVertex, which no vertex id equals
         for (uint32_t i = 0; i < n; i++) {
             const uint32_t v = i < n_row ? rows_s[i * 32 + j] : x;
-            found += (s.y == v) + (s.x > 1 && s.z == v) + (s.x > 2 && s.w == v);
+            found += (s.y == v) + (s.z == v) + (s.w == v);
         }
         return found;
     }

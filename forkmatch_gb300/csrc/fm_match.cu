@@ -374,6 +374,7 @@ __device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpM
                                               const uint8_t* col_depth_s, uint32_t& nst,
                                               unsigned long long& n_count, PreAcc& pre) {
     const uint32_t pbase = chunk * 32;
+    unsigned long long lane_count = 0;   // pre-count: this lane's counts, summed over the warp at the end
     for (uint32_t base = begin; base < end; base += 32 * kSlots) {
         uint32_t j[kSlots], t[kSlots], x[kSlots];
         bool ok[kSlots];
@@ -412,7 +413,7 @@ __device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpM
                     pre.parents += 1;
                     pre.words += sg.x;
                 }
-                n_count += dev::warp_sum_u32(c);
+                lane_count += c;
             }
             continue;
         }
@@ -438,6 +439,11 @@ __device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpM
             nst = 0;
         }
         __syncwarp();
+    }
+    if (MODE == kModeLastCount && !DUPS && P.pre_count) {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) lane_count += __shfl_xor_sync(kFull, lane_count, o);
+        n_count += lane_count;
     }
 }
 
