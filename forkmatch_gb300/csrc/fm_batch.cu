@@ -78,6 +78,7 @@ struct BatchParams {
     uint32_t max_warps;
     uint32_t piece_shift;                     // autotuned: heavy threshold and piece size scale
     uint32_t stage_words;                     // per-warp membership-list stage (0: lists stay in global memory)
+    uint32_t self_loops;                      // the graph has an e-line v -> v (see ExpandParams)
 };
 
 namespace {
@@ -359,7 +360,7 @@ __device__ __forceinline__ void bprecount(const BatchParams& P, const BMem& m, b
         const uint32_t rb = pl.req_begin[d + 1];
         const uint32_t anc = pl.req_anc[rb];
         const uint4 sg = ldg4(P.seg + (uint64_t)pl.req_label[rb] * P.V + (anc == d ? x : m.rows_s[anc * 32 + j]));
-        c = sg.x - dev::count_members(sg, m.rows_s, j, d, x, true, P.nbr, P.bm, P.bm_words);
+        c = sg.x - dev::count_members(sg, m.rows_s, j, d, x, P.self_loops || anc != d, P.nbr, P.bm, P.bm_words);
     }
     const unsigned grp = __match_any_sync(kFull, qid);
     const unsigned lo = __reduce_add_sync(grp, c & 0xffffu);
@@ -1362,6 +1363,7 @@ fm_status fm_batch_run(fm_batch* b, uint64_t* counts, fm_batch_stats* stats) {
         run.base.heavy_cap = cv.heavy_cap;
         run.base.piece_shift = b->piece_shift;
         run.base.stage_words = stage_words_knob();
+        run.base.self_loops = g.has_self_loops ? 1u : 0u;
         if ((uint64_t)nq * run.base.chunks_per_query >= (1ull << 32)) {
             set_error("too many (query, root chunk) pairs in one batch; split the batch");
             return FM_ERR_UNSUPPORTED;

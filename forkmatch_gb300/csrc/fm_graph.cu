@@ -19,12 +19,14 @@ namespace {
 
 __global__ void k_make_keys(const uint32_t* __restrict__ src, const uint32_t* __restrict__ dst,
                             const uint32_t* __restrict__ lab, uint64_t E, uint32_t V, uint32_t L,
-                            uint32_t vbits, uint64_t* __restrict__ keys, unsigned int* err) {
+                            uint32_t vbits, uint64_t* __restrict__ keys, unsigned int* err, unsigned int* loops) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < E; i += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t s = src[i], d = dst[i], l = lab[i];
         if (s >= V || d >= V || l >= L) {
             atomicOr(err, 1u);
             s = d = l = 0;
+        } else if (s == d) {
+            atomicOr(loops, 1u);
         }
         keys[i] = ((uint64_t)l << (2 * vbits)) | ((uint64_t)s << vbits) | (uint64_t)d;
     }
@@ -236,12 +238,13 @@ fm_status build_device_graph(DeviceGraph& g, uint32_t V, uint32_t L, uint64_t E,
     FM_CUDA(cudaMalloc(&g.seg, (size_t)L * V * sizeof(uint4)));
     FM_CUDA(cudaMemsetAsync(g.seg, 0, (size_t)L * V * sizeof(uint4), s));
 
-    DevBuf flags;   // [0] error, [1] dup, [2] max_len, [3..4] nlong
+    DevBuf flags;   // [0] error, [1] dup, [2] max_len, [3] self-loop seen, [4..5] nlong
     FM_CUDA(cudaMalloc(&flags.p, 64));
     FM_CUDA(cudaMemsetAsync(flags.p, 0, 64, s));
     unsigned int* d_err = flags.as<unsigned int>();
     unsigned int* d_dup = d_err + 1;
     unsigned int* d_max = d_err + 2;
+    unsigned int* d_loops = d_err + 3;
     unsigned long long* d_nlong = (unsigned long long*)(d_err + 4);
 
     uint64_t nseg = 0, total16 = 0;
@@ -249,7 +252,8 @@ fm_status build_device_graph(DeviceGraph& g, uint32_t V, uint32_t L, uint64_t E,
         DevBuf keys, keys_alt, temp, head, incl;
         FM_CUDA(cudaMalloc(&keys.p, E * 8));
         FM_CUDA(cudaMalloc(&keys_alt.p, E * 8));
-        k_make_keys<<<grid_for(E, sms), 256, 0, s>>>(d_src, d_dst, d_lab, E, V, L, vbits, keys.as<uint64_t>(), d_err);
+        k_make_keys<<<grid_for(E, sms), 256, 0, s>>>(d_src, d_dst, d_lab, E, V, L, vbits, keys.as<uint64_t>(), d_err,
+                                                     d_loops);
         FM_CUDA(cudaGetLastError());
         cub::DoubleBuffer<uint64_t> db(keys.as<uint64_t>(), keys_alt.as<uint64_t>());
         size_t tb = 0;
@@ -390,6 +394,7 @@ fm_status build_device_graph(DeviceGraph& g, uint32_t V, uint32_t L, uint64_t E,
         return FM_ERR_DATA_LINE;
     }
     g.has_dups = hflags[1] ? 1 : 0;
+    g.has_self_loops = hflags[3] ? 1 : 0;
     g.max_len = hflags[2];
     g.segments = nseg;
     g.long_segments = nlong;

@@ -936,6 +936,7 @@ fm_status match_impl(fm_context* ctx, const fm_graph* graph, const fm_query* que
         b.work_limit = opts.work_limit;
         b.stage_words = stage_words_knob();
         b.pre_count = run.pre ? 1u : 0u;
+        b.self_loops = g.has_self_loops ? 1u : 0u;
         out->pre_counted = run.pre ? 1 : 0;
         run.work_limit = opts.work_limit;
         fm_status st = FM_ERR_UNSUPPORTED;

@@ -59,6 +59,7 @@ struct DeviceGraph {
     uint64_t segments = 0, long_segments = 0;
     uint32_t max_len = 0;
     int has_dups = 0;
+    int has_self_loops = 0;    // some e-line has src == dst
     int device = 0;
     double build_ms = 0;
     std::vector<uint64_t> label_count;   // e-lines per label slot
@@ -198,6 +199,9 @@ struct ExpandParams {
     // counters (parents, lookups, list words) are added to ctl[1] of the
     // counting level's control block array (the next depth's block).
     uint32_t pre_count;
+    // The graph has an e-line v -> v: only then can a vertex be in its own
+    // list, so only then does pre-count test the new vertex against its list.
+    uint32_t self_loops;
 };
 constexpr unsigned int kLimitFlag = 2u;
 

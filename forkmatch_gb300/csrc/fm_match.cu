@@ -409,7 +409,8 @@ __device__ __forceinline__ void process_slots(const ExpandParams& P, const WarpM
                 uint32_t c = 0;
                 if (ok[u]) {
                     const uint4 sg = ldg4(segl + (anc == d ? x[u] : m.rows_s[anc * 32 + j[u]]));
-                    c = sg.x - dev::count_members(sg, m.rows_s, j[u], d, x[u], true, P.nbr, P.bm, P.bm_words);
+                    c = sg.x - dev::count_members(sg, m.rows_s, j[u], d, x[u], P.self_loops || anc != d, P.nbr,
+                                                  P.bm, P.bm_words);
                     pre.parents += 1;
                     pre.words += sg.x;
                 }
