@@ -1,6 +1,8 @@
 """Benchmark: embeddings/sec of batched matching (512 queries in shared
-launches replayed as a CUDA graph) beside the plain form (one query per
-launch sequence), on the batched workload, with full uint32 embedding tables.
+launches replayed as a CUDA graph, the queries whose work fills the GPU alone
+matched alone inside the run, as the autotuner picks) beside the plain form
+(one fm_match per query), on the batched workload, with full uint32 embedding
+tables for the table queries and u64 counts for the count-only ones.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --workload plain_at_scale|plain_small|serving|skew|ingest
