@@ -808,7 +808,10 @@ def run_batched(args, rank, world, local):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "traffic": batched_traffic(alg_bytes / max(1, world) - alg_alone, alg_alone),
-                         "kernel": "k_bexpand + k_bexpand_heavy (one batch run; k_bpersist when the tuner picks the persistent engine)",
+                         "kernel": "one batch run: k_bexpand + k_bexpand_heavy for the shared launches (k_bpersist "
+                                   "when the tuner picks the persistent engine), k_expand + k_expand_heavy for the "
+                                   "queries matched alone (the dominant one: the pre-count level of the 5-vertex "
+                                   "count-only paths)",
                          "peak_kind": peak_kind, "algorithmic_bytes_per_step": alg_bytes,
                          "traffic_source": "profiles/k_bexpand_batched.md (DRAM bytes per algorithmic byte of "
                                            "the batch kernels and of the single-query kernels, captured on every "
